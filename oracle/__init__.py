@@ -1,0 +1,5 @@
+"""CPU oracle for the visibility simulator (test infrastructure only; see
+``oracle/vis_oracle.py``).  Never imported by the product package."""
+from .vis_oracle import (SPEED_OF_LIGHT, bilinear_beam, phasors,  # noqa: F401
+                         hermitian_product, vis_oracle, vis_oracle_partial,
+                         rel_frobenius)
