@@ -1,0 +1,9 @@
+"""GB300-native drop-in for hera_gpu's visibility simulator (``vis_gpu``).
+
+The compute path is libheravis.so (hand-written sm_103a CUDA behind the C ABI
+of include/heravis.h), loaded through ctypes; there is no CPU fallback.
+"""
+name = "hera_gpu_gb300"
+
+from .vis import vis_gpu, vis_gpu_multifreq  # noqa: E402,F401
+from ._native import Context, HeraVisError, default_context  # noqa: E402,F401

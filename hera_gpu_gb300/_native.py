@@ -1,0 +1,181 @@
+"""ctypes binding of libheravis.so (the C ABI declared in include/heravis.h).
+
+The library is the only compute path: if it is missing, or no CUDA device is
+usable, every call raises -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+import weakref
+
+import numpy as np
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libheravis.so")
+
+HV_OK = 0
+HV_ERR_ARG = 1
+HV_ERR_OOM = 2
+HV_ERR_CUDA = 3
+HV_ERR_TIMEOUT = 4
+HV_ERR_UNSUPPORTED = 5
+
+METHODS = {"auto": 0, "plain": 1, "tc": 2, "tc_bf16": 2}
+
+# Every function of the ABI: name -> (restype, argtypes)
+_c_int, _c_void_p, _c_size_t, _c_double = ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_double
+_PTR = ctypes.c_void_p
+SIGNATURES = {
+    "hv_version": (_c_int, []),
+    "hv_create": (_c_int, [ctypes.POINTER(_c_void_p), _c_int, _c_size_t]),
+    "hv_destroy": (_c_int, [_c_void_p]),
+    "hv_last_error": (ctypes.c_char_p, [_c_void_p]),
+    "hv_launch_count": (ctypes.c_uint64, [_c_void_p]),
+    "hv_vis_gpu": (_c_int, [_c_void_p, _c_int, _c_int, _PTR, _c_int, _c_double, _PTR, _c_int,
+                            _PTR, _PTR, _c_int, _PTR, _c_int, _PTR]),
+    "hv_vis_multifreq": (_c_int, [_c_void_p, _c_int, _c_int, _PTR, _c_int, _PTR, _c_int, _PTR,
+                                  _c_int, _PTR, _PTR, _c_int, _PTR, _c_int, _PTR]),
+    "hv_vis_multifreq_device": (_c_int, [_c_void_p, _c_int, _c_int, _PTR, _c_int, _PTR, _c_int,
+                                         _PTR, _c_int, _PTR, _PTR, _c_int, _PTR, _c_int, _PTR,
+                                         _c_void_p]),
+    "hv_sync": (_c_int, [_c_void_p]),
+    "hv_host_alloc": (_c_int, [_c_void_p, _c_size_t, ctypes.POINTER(_c_void_p)]),
+    "hv_host_free": (_c_int, [_c_void_p, _c_void_p]),
+}
+
+
+class HeraVisError(RuntimeError):
+    """A failed library call; ``code`` is the hv_status."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"[hv_status {code}] {msg}")
+        self.code = code
+
+
+class HeraVisArgumentError(HeraVisError, AssertionError):
+    """Bad shape or argument (the reference raises AssertionError here)."""
+
+
+class HeraVisTimeout(HeraVisError):
+    """A bounded device-side wait gave up; the GPU context stays usable."""
+
+
+_lib = None
+_lib_lock = threading.Lock()
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libheravis.so and declare its ABI.  Raises if it is missing."""
+    global _lib
+    with _lib_lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(path):
+            raise RuntimeError(
+                f"libheravis.so not found at {path}: build it with "
+                "`python -m hera_gpu_gb300.build` (nvcc, sm_103a). There is no CPU fallback.")
+        lib = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else ctypes.c_void_p(0)
+
+
+class Context:
+    """One hv_context: a CUDA device, a stream and a workspace."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        rc = self.lib.hv_create(ctypes.byref(h), int(device), int(hbm_budget_bytes))
+        if rc != HV_OK:
+            if rc == HV_ERR_UNSUPPORTED:
+                raise HeraVisError(rc, "no CUDA device available: libheravis needs a GB300 GPU")
+            raise HeraVisError(rc, f"hv_create(device={device}) failed")
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.hv_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, rc):
+        if rc == HV_OK:
+            return
+        msg = self.lib.hv_last_error(self.h).decode(errors="replace")
+        if rc == HV_ERR_ARG:
+            raise HeraVisArgumentError(rc, msg)
+        if rc == HV_ERR_TIMEOUT:
+            raise HeraVisTimeout(rc, msg)
+        raise HeraVisError(rc, msg)
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.hv_launch_count(self.h))
+
+    def sync(self):
+        self.check(self.lib.hv_sync(self.h))
+
+    def vis_multifreq(self, precision, method, antpos, freqs, eq2tops, crd_eq, I_sky, bm_cubes, out):
+        """Host arrays in, host array ``out`` (nfreq, ntimes, nant, nant) written."""
+        freqs = np.ascontiguousarray(freqs, dtype=np.float64)
+        nant = antpos.shape[0]
+        rc = self.lib.hv_vis_multifreq(
+            self.h, int(precision), METHODS[method], _ptr(antpos), nant, _ptr(freqs), len(freqs),
+            _ptr(eq2tops), eq2tops.shape[0], _ptr(crd_eq), _ptr(I_sky), crd_eq.shape[1],
+            _ptr(bm_cubes), bm_cubes.shape[-1], _ptr(out))
+        self.check(rc)
+        return out
+
+    def vis_multifreq_device(self, precision, method, d_antpos, nant, freqs, d_eq2tops, ntimes,
+                             d_crd_eq, d_I_sky, nsrc, d_bm_cubes, beam_px, d_out, stream=0):
+        """Device pointers (ints) in and out; asynchronous on ``stream``."""
+        freqs = np.ascontiguousarray(freqs, dtype=np.float64)
+        rc = self.lib.hv_vis_multifreq_device(
+            self.h, int(precision), METHODS[method], ctypes.c_void_p(d_antpos), int(nant),
+            _ptr(freqs), len(freqs), ctypes.c_void_p(d_eq2tops), int(ntimes),
+            ctypes.c_void_p(d_crd_eq), ctypes.c_void_p(d_I_sky), int(nsrc),
+            ctypes.c_void_p(d_bm_cubes), int(beam_px), ctypes.c_void_p(d_out),
+            ctypes.c_void_p(stream))
+        self.check(rc)
+
+    def pinned_empty(self, shape, dtype):
+        """A numpy array in page-locked host memory, freed when the last view
+        of it is gone."""
+        dtype = np.dtype(dtype)
+        n = int(np.prod(shape))
+        nbytes = max(n * dtype.itemsize, 1)
+        p = ctypes.c_void_p()
+        self.check(self.lib.hv_host_alloc(self.h, nbytes, ctypes.byref(p)))
+        buf = (ctypes.c_byte * nbytes).from_address(p.value)
+        weakref.finalize(buf, self.lib.hv_host_free, self.h, ctypes.c_void_p(p.value))
+        return np.frombuffer(buf, dtype=dtype, count=n).reshape(shape)
+
+
+_contexts = {}
+_ctx_lock = threading.Lock()
+
+
+def default_context(device: int = 0) -> Context:
+    """Process-wide context per device, created on first use (the reference
+    binds device 0 at import through pycuda.autoinit, vis.py:1)."""
+    with _ctx_lock:
+        ctx = _contexts.get(device)
+        if ctx is None:
+            ctx = Context(device)
+            _contexts[device] = ctx
+        return ctx

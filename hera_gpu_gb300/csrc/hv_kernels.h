@@ -1,0 +1,83 @@
+// hv_kernels.h -- host-side launchers of the kernels of libheravis.so
+// (internal to the library; the public C ABI is include/heravis.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace hv {
+
+// --- hv_prep.cu ------------------------------------------------------------
+// bm (nfreq, nant, P, P) -> beamT (nfreq, P*P, Np), zero for padded antennas.
+template <typename R>
+cudaError_t launch_beam_transpose(const R* bm, int nfreq, int nant, int P, int Np,
+                                  R* beamT, cudaStream_t st);
+
+// Phase coefficients for times [t0, t0 + nt) and every frequency:
+// U[(tt * nfreq + f) * Np + a].
+template <typename R>
+cudaError_t launch_ucoef(const R* antpos, int nant, int Np, const R* eq2tops, int t0,
+                         int nt, const double* d_freqs, int nfreq, void* U,
+                         cudaStream_t st);
+
+// Number of prep blocks for nsrc sources.
+int prep_blocks(int nsrc);
+
+// Horizon cut + beam corner for times [t0, t0 + nt): records of the sources
+// with z > 0, in input order, into rec + tt * nsrc; counts into count[tt].
+// block_counts needs prep_blocks(nsrc) * nt ints.
+template <typename R>
+cudaError_t launch_prep(const R* crd_eq, const R* I_sky, int nsrc, const R* eq2tops,
+                        int t0, int nt, int P, int* block_counts, void* rec,
+                        int* count, cudaStream_t st);
+
+// --- hv_plain.cu -----------------------------------------------------------
+// Source chunk of the split-K sum over sources (plain path).
+constexpr int kPlainChunk = 4096;
+
+// v[s][a] (complex, Np per source) for the count[0] records of one slice.
+template <typename R>
+cudaError_t launch_gen_phasors(const void* rec, const int* count, int nsrc_max,
+                               const void* U, const R* beamT, int Np, int nant, int P,
+                               void* v, cudaStream_t st);
+
+// Upper-triangle SIMT Hermitian product of v into partial sums, one chunk of
+// kPlainChunk sources per grid row.
+template <typename R>
+cudaError_t launch_herk_plain(const void* v, const int* count, int nsrc_max, int Np,
+                              R* partial, cudaStream_t st);
+
+// For each of nt * nf slices (slice = tl * nf + f, partial sums at
+// partial + slice * slice_stride, source count counts[tl]): sum the valid
+// chunks (ceil(count / chunk) of them) in order and write the full Hermitian
+// matrix (nant x nant complex R, row-major) to
+// out + ((f * ntimes_out) + t0 + tl) * nant * nant.
+template <typename R>
+cudaError_t launch_reduce(const R* partial, size_t slice_stride, const int* counts, int nt,
+                          int nf, int t0, int ntimes_out, int chunk, int Np, int nant, void* out,
+                          cudaStream_t st);
+
+// --- hv_tc.cu --------------------------------------------------------------
+struct TcLaunch {
+  const void* rec;      // SrcRec32 [nt][nsrc]
+  const int* counts;    // [nt]
+  int nsrc, nt, nf;
+  const void* U;        // Ucoef32 [nt][nf][Np]
+  const float* beamT;   // [nf][P*P][Np]
+  int Np, nant, P;
+  float* partial;       // [nt * nf][ceil(nsrc / chunk)][2][Np][Np]
+  int chunk;            // sources per split-K chunk (multiple of 32)
+  const void* groups;   // device copy of the group table (tc_fill_group_table)
+  int ngroups, max_slots;
+  int* err;             // device error flag
+  int num_sms;
+};
+cudaError_t launch_tc(const TcLaunch& L, cudaStream_t st);
+size_t tc_partial_floats(int Np, int nsrc, int nslices, int chunk);
+int tc_chunk_sources(int nsrc, int nslices, int ngroups, int num_sms);
+size_t tc_group_table_bytes(int nant);
+int tc_fill_group_table(int nant, void* host_buf);
+int tc_max_slots(int nant);
+
+}  // namespace hv

@@ -1,0 +1,251 @@
+// hv_prep.cu -- per-call and per-time preparation kernels.
+//
+//  * beam transpose: the reference uploads bm_cube into a 3-D texture
+//    (hera_gpu/vis.py:113-138, 198); here the beam stays in global memory as
+//    [pixel][antenna] so that a warp whose lanes are antennas gathers one
+//    128-byte line per beam corner.
+//  * phase coefficients: the reference forms tau = antpos . (eq2top . crd_eq)
+//    / c with two GEMMs per chunk (vis.py:230-235) and multiplies by 2 pi nu
+//    in MeasEq (vis.py:107).  Since p . (R s) = (R^T p) . s, the per-antenna
+//    vector U = nu / c * R^T p is formed once per (time, frequency) in FP64
+//    and the phase in cycles is U . s_eq.
+//  * source prep: rotation to topocentric, horizon cut (vis.py:75, 85-86) and
+//    the bilinear corner / weights (vis.py:63-73), once per time and shared
+//    by every antenna and frequency.  Sources below the horizon are dropped
+//    (the reference computes them and multiplies by A = 0); the survivors keep
+//    their input order, so the split-K order is deterministic.
+#include "hv_internal.cuh"
+#include "hv_kernels.h"
+
+namespace hv {
+
+// ---------------------------------------------------------------- beam ----
+template <typename R>
+__global__ void beam_transpose_kernel(const R* __restrict__ bm, int nant, int PP, int Np,
+                                      R* __restrict__ beamT) {
+  __shared__ R tile[32][33];
+  const int f = blockIdx.z;
+  const int pix0 = blockIdx.x * 32, a0 = blockIdx.y * 32;
+  const R* src = bm + (size_t)f * nant * PP;
+  R* dst = beamT + (size_t)f * PP * Np;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int a = a0 + j, pix = pix0 + threadIdx.x;
+    tile[j][threadIdx.x] = (a < nant && pix < PP) ? src[(size_t)a * PP + pix] : R(0);
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int pix = pix0 + j, a = a0 + threadIdx.x;
+    if (pix < PP && a < Np) dst[(size_t)pix * Np + a] = tile[threadIdx.x][j];
+  }
+}
+
+template <typename R>
+cudaError_t launch_beam_transpose(const R* bm, int nfreq, int nant, int P, int Np,
+                                  R* beamT, cudaStream_t st) {
+  const int PP = P * P;
+  dim3 grid(ceil_div(PP, 32), Np / 32, nfreq), block(32, 8);
+  beam_transpose_kernel<R><<<grid, block, 0, st>>>(bm, nant, PP, Np, beamT);
+  return cudaGetLastError();
+}
+
+// ----------------------------------------------------------- U coeffs ----
+__device__ __forceinline__ void store_ucoef(Ucoef32* U, size_t i, const double u[3]) {
+  Ucoef32 c;
+  c.hx = (float)u[0]; c.hy = (float)u[1]; c.hz = (float)u[2]; c.p0 = 0.f;
+  c.lx = (float)(u[0] - (double)c.hx);
+  c.ly = (float)(u[1] - (double)c.hy);
+  c.lz = (float)(u[2] - (double)c.hz);
+  c.p1 = 0.f;
+  U[i] = c;
+}
+__device__ __forceinline__ void store_ucoef(Ucoef64* U, size_t i, const double u[3]) {
+  Ucoef64 c;
+  c.x = u[0]; c.y = u[1]; c.z = u[2]; c.p = 0.0;
+  U[i] = c;
+}
+
+template <typename R>
+__global__ void ucoef_kernel(const R* __restrict__ antpos, int nant, int Np,
+                             const R* __restrict__ eq2tops, int t0, int nt,
+                             const double* __restrict__ freqs, int nfreq,
+                             typename Traits<R>::U* __restrict__ U) {
+  const size_t total = (size_t)nt * nfreq * Np;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int a = (int)(i % Np);
+    const int f = (int)((i / Np) % nfreq);
+    const int tt = (int)(i / ((size_t)Np * nfreq));
+    double u[3] = {0.0, 0.0, 0.0};
+    if (a < nant) {
+      const R* M = eq2tops + (size_t)(t0 + tt) * 9;
+      const double p0 = antpos[a * 3 + 0], p1 = antpos[a * 3 + 1], p2 = antpos[a * 3 + 2];
+      const double scale = freqs[f] / kSpeedOfLight;
+      for (int k = 0; k < 3; ++k) {
+        // (R^T p)_k = sum_j R[j][k] p_j
+        const double w = fma((double)M[0 * 3 + k], p0,
+                             fma((double)M[1 * 3 + k], p1, (double)M[2 * 3 + k] * p2));
+        u[k] = w * scale;
+      }
+    }
+    store_ucoef(U, i, u);
+  }
+}
+
+template <typename R>
+cudaError_t launch_ucoef(const R* antpos, int nant, int Np, const R* eq2tops, int t0,
+                         int nt, const double* d_freqs, int nfreq, void* U,
+                         cudaStream_t st) {
+  const size_t total = (size_t)nt * nfreq * Np;
+  const int blocks = (int)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
+  ucoef_kernel<R><<<blocks > 0 ? blocks : 1, 256, 0, st>>>(
+      antpos, nant, Np, eq2tops, t0, nt, d_freqs, nfreq,
+      reinterpret_cast<typename Traits<R>::U*>(U));
+  return cudaGetLastError();
+}
+
+// -------------------------------------------------------- source prep ----
+int prep_blocks(int nsrc) { return nsrc > 0 ? ceil_div(nsrc, kPrepBlock) : 1; }
+
+template <typename R>
+__device__ __forceinline__ void load_rot(const R* __restrict__ eq2tops, int t, double* rot) {
+  if (threadIdx.x < 9) rot[threadIdx.x] = (double)eq2tops[(size_t)t * 9 + threadIdx.x];
+}
+
+// z component of eq2top . s (topocentric up), FP64.
+__device__ __forceinline__ double top_z(const double* rot, double x, double y, double z) {
+  return fma(rot[6], x, fma(rot[7], y, rot[8] * z));
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kPrepBlock)
+prep_count_kernel(const R* __restrict__ crd_eq, int nsrc, const R* __restrict__ eq2tops,
+                  int t0, int nblk, int* __restrict__ block_counts) {
+  __shared__ double rot[9];
+  __shared__ int warp_cnt[kPrepBlock / 32];
+  const int tt = blockIdx.y;
+  load_rot(eq2tops, t0 + tt, rot);
+  __syncthreads();
+  const int s = blockIdx.x * kPrepBlock + threadIdx.x;
+  bool up = false;
+  if (s < nsrc)
+    up = top_z(rot, crd_eq[s], crd_eq[(size_t)nsrc + s], crd_eq[2 * (size_t)nsrc + s]) > 0.0;
+  const unsigned m = __ballot_sync(0xffffffffu, up);
+  if ((threadIdx.x & 31) == 0) warp_cnt[threadIdx.x >> 5] = __popc(m);
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int c = warp_cnt[threadIdx.x];
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (threadIdx.x == 0) block_counts[(size_t)tt * nblk + blockIdx.x] = c;
+  }
+}
+
+__device__ __forceinline__ void fill_rec(SrcRec32& r, double x, double y, double z,
+                                         double amp, int pix, double fx, double fy) {
+  r.sx = (float)x; r.sy = (float)y; r.sz = (float)z; r.amp = (float)amp;
+  r.pix = pix; r.fx = (float)fx; r.fy = (float)fy; r.pad = 0;
+}
+__device__ __forceinline__ void fill_rec(SrcRec64& r, double x, double y, double z,
+                                         double amp, int pix, double fx, double fy) {
+  r.sx = x; r.sy = y; r.sz = z; r.amp = amp; r.fx = fx; r.fy = fy; r.pix = pix;
+  r.pad[0] = r.pad[1] = r.pad[2] = 0;
+}
+
+// Lower corner and weight along one beam axis, clamped so that the four
+// gathered texels always lie inside the P x P grid.  Outside the grid the
+// value is the edge texel's, as with the reference's clamped texture
+// (vis.py:39) and RectBivariateSpline (test_vis_gpu.py:334).
+__device__ __forceinline__ int beam_axis(double c, int P, double& w) {
+  const double b = (P - 1) * fma(0.5, c, 0.5);
+  const double fb = floor(b);
+  w = b - fb;
+  if (P < 2) { w = 0.0; return 0; }
+  if (fb < 0.0) w = 0.0;
+  if (fb >= (double)(P - 1)) w = 1.0;
+  return (int)fmin(fmax(fb, 0.0), (double)(P - 2));
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kPrepBlock)
+prep_write_kernel(const R* __restrict__ crd_eq, const R* __restrict__ I_sky, int nsrc,
+                  const R* __restrict__ eq2tops, int t0, int nblk, int P,
+                  const int* __restrict__ block_counts,
+                  typename Traits<R>::Rec* __restrict__ rec, int* __restrict__ count) {
+  __shared__ double rot[9];
+  __shared__ int warp_cnt[kPrepBlock / 32];
+  __shared__ int red[kPrepBlock / 32];
+  __shared__ int base;
+  const int tt = blockIdx.y;
+  const int* bc = block_counts + (size_t)tt * nblk;
+  load_rot(eq2tops, t0 + tt, rot);
+  // offset of this block = sum of the counts of the blocks before it
+  int part = 0;
+  for (int i = threadIdx.x; i < (int)blockIdx.x; i += kPrepBlock) part += bc[i];
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int c = red[threadIdx.x];
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (threadIdx.x == 0) base = c;
+  }
+  const int s = blockIdx.x * kPrepBlock + threadIdx.x;
+  double x = 0, y = 0, z = 0, tx = 0, ty = 0, tz = 0;
+  bool up = false;
+  __syncthreads();
+  if (s < nsrc) {
+    x = crd_eq[s]; y = crd_eq[(size_t)nsrc + s]; z = crd_eq[2 * (size_t)nsrc + s];
+    tx = fma(rot[0], x, fma(rot[1], y, rot[2] * z));
+    ty = fma(rot[3], x, fma(rot[4], y, rot[5] * z));
+    tz = top_z(rot, x, y, z);
+    up = tz > 0.0;
+  }
+  const unsigned m = __ballot_sync(0xffffffffu, up);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) warp_cnt[warp] = __popc(m);
+  __syncthreads();
+  if (warp == 0) {  // exclusive scan of the warp counts
+    const int c = warp_cnt[lane];
+    int incl = c;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int n = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += n;
+    }
+    red[lane] = incl - c;
+    if (blockIdx.x == nblk - 1 && lane == 31) count[tt] = base + incl;
+  }
+  __syncthreads();
+  if (up) {
+    const int idx = base + red[warp] + __popc(m & ((1u << lane) - 1u));
+    double fx, fy;
+    const int px = beam_axis(tx, P, fx);
+    const int py = beam_axis(ty, P, fy);
+    typename Traits<R>::Rec r;
+    fill_rec(r, x, y, z, sqrt((double)I_sky[s]), py * P + px, fx, fy);
+    rec[(size_t)tt * nsrc + idx] = r;
+  }
+}
+
+template <typename R>
+cudaError_t launch_prep(const R* crd_eq, const R* I_sky, int nsrc, const R* eq2tops,
+                        int t0, int nt, int P, int* block_counts, void* rec,
+                        int* count, cudaStream_t st) {
+  const int nblk = prep_blocks(nsrc);
+  dim3 grid(nblk, nt);
+  prep_count_kernel<R><<<grid, kPrepBlock, 0, st>>>(crd_eq, nsrc, eq2tops, t0, nblk,
+                                                    block_counts);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  prep_write_kernel<R><<<grid, kPrepBlock, 0, st>>>(
+      crd_eq, I_sky, nsrc, eq2tops, t0, nblk, P, block_counts,
+      reinterpret_cast<typename Traits<R>::Rec*>(rec), count);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_beam_transpose<float>(const float*, int, int, int, int, float*, cudaStream_t);
+template cudaError_t launch_beam_transpose<double>(const double*, int, int, int, int, double*, cudaStream_t);
+template cudaError_t launch_ucoef<float>(const float*, int, int, const float*, int, int, const double*, int, void*, cudaStream_t);
+template cudaError_t launch_ucoef<double>(const double*, int, int, const double*, int, int, const double*, int, void*, cudaStream_t);
+template cudaError_t launch_prep<float>(const float*, const float*, int, const float*, int, int, int, int*, void*, int*, cudaStream_t);
+template cudaError_t launch_prep<double>(const double*, const double*, int, const double*, int, int, int, int*, void*, int*, cudaStream_t);
+
+}  // namespace hv

@@ -1,0 +1,672 @@
+// hv_tc.cu -- the fused tensor-core form of the hot path (sm_103a).
+//
+// One persistent kernel replaces the reference's per-chunk sequence
+// SGEMM rotation -> SGEMM delay -> InterpolateBeam -> MeasEq -> CGEMM
+// (hera_gpu/vis.py:224-250).  Phasors v[a, s] never leave the SM: they are
+// generated straight into shared memory as split-BF16 operand tiles and
+// contracted on the tensor cores (tcgen05.mma, FP32 accumulators in TMEM).
+//
+// Work decomposition
+//   Antennas are cut into blocks of 128 (the MMA M).  The upper triangle of
+//   block pairs (I <= J) is partitioned into groups of at most two pairs that
+//   touch at most three blocks ("slots"); a group's accumulators -- Re V and
+//   Im V for each pair, 128 x 128 FP32 each -- fill the 512 TMEM columns.
+//   A work item is (time, frequency, source chunk, group).  Items are taken
+//   round-robin by a grid of one CTA per SM; each item's partial sum over its
+//   source chunk goes to HBM and a separate kernel reduces the chunks in a
+//   fixed order (deterministic split-K over sources).
+//
+// Pipeline inside a CTA (576 threads)
+//   warp 16       TMA producer: 32 source records per stage, one 2-D
+//                 cp.async.bulk.tensor into shared memory.
+//   warps 0-15    phasor generators: for each (slot, antenna row, 8 sources)
+//                 the bilinear beam (4 coalesced gathers: lanes are
+//                 antennas), the phase in cycles reduced exactly in FP32
+//                 (phase_cycles32), sincos, v = A sqrt(I) e^{2 pi i phi},
+//                 split v = hi + lo in BF16, stored to the canonical K-major
+//                 128-byte-swizzled UMMA layout.  After the last stage of an
+//                 item they drain TMEM to the partial buffer (epilogue).
+//   warp 17       MMA issuer (one thread) and TMEM owner.
+//
+// Operand layout of one stage (32 sources, K = 64 BF16 per antenna row):
+//   K chunks of 16 bytes: [Re s0-7, Re s8-15, Im s0-7, Im s8-15,
+//                          Re s16-23, Re s24-31, Im s16-23, Im s24-31]
+//   so each MMA K-step (16 elements) holds either the real or the imaginary
+//   parts of 16 sources, and per K half h (16 sources):
+//     ReV += ReA ReB^T + ImA ImB^T,   ImV += ImA ReB^T - ReA ImB^T
+//   (V[a,b] = sum_s v_a conj(v_b)); the minus sign is the instruction
+//   descriptor's negate-A bit.  Split BF16 keeps hi*hi + hi*lo + lo*hi.
+//
+// Every wait on an mbarrier is bounded in time; on expiry the kernel raises
+// an error flag, lets in-flight copies and MMAs land (again bounded), frees
+// TMEM and returns, so the host sees HV_ERR_TIMEOUT instead of a hung GPU.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "hv_internal.cuh"
+#include "hv_kernels.h"
+
+namespace hv {
+
+constexpr int TC_ROWS = 128;          // antennas per block = MMA M
+constexpr int TC_KS = 32;             // sources per stage
+constexpr int TC_HALF = 16384;        // one operand tile: 128 rows x 128 B
+constexpr int TC_SLOT = 2 * TC_HALF;  // hi + lo tiles of one block
+constexpr int TC_REC = TC_KS * 32;    // bytes of source records per stage
+constexpr int TC_GEN_WARPS = 16;
+constexpr int TC_GEN_THREADS = TC_GEN_WARPS * 32;
+constexpr int TC_PRODUCER_WARP = TC_GEN_WARPS;
+constexpr int TC_MMA_WARP = TC_GEN_WARPS + 1;
+constexpr int TC_THREADS = TC_GEN_THREADS + 64;
+constexpr int TC_TMEM_COLS = 512;
+constexpr int TC_SMEM_LIMIT = 227 * 1024;
+constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // 2 s per wait
+
+constexpr int kErrTimeout = 1;
+
+struct TcGroup {
+  int npairs, nslots;
+  int slot_block[3];
+  int slot_rows[3];  // valid antenna rows of each slot's block
+  int pa[2], pb[2];  // slots of the row (A) and column (B) operands of each pair
+  int pI[2], pJ[2];  // block indices of each pair
+  int pN[2];         // MMA N of each pair (valid columns of block J, multiple of 16)
+};
+
+struct TcParams {
+  const int* counts;    // [nt] sources above the horizon per time
+  int nsrc;             // records per time in the record tensor
+  int nt, nf;           // times and frequencies of this launch
+  const Ucoef32* U;     // [nt][nf][Np]
+  const float* beamT;   // [nf][PP][Np]
+  int Np, nant, PP, dx, dy;
+  float* partial;       // [nt * nf][nchunk][2][Np][Np]
+  int nchunk, chunk;
+  const TcGroup* groups;
+  int ngroups;
+  int nstages, max_slots;
+  int* err;
+  long long total_items;
+};
+
+// ------------------------------------------------------------ PTX helpers --
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Single-thread bounded wait.
+__device__ __forceinline__ bool wait1(uint32_t bar, uint32_t parity, volatile int* abort_flag,
+                                      int* gerr) {
+  const unsigned long long t0 = global_ns();
+  for (uint32_t i = 0;; ++i) {
+    if (mbar_try(bar, parity)) return true;
+    if ((i & 63) == 63) {
+      if (*abort_flag) return false;
+      if (global_ns() - t0 > TC_WAIT_NS) {
+        *abort_flag = 1;
+        atomicExch(gerr, kErrTimeout);
+        return false;
+      }
+    }
+  }
+}
+
+// Whole-warp bounded wait; the outcome is uniform across the warp.
+__device__ __forceinline__ bool wait_warp(uint32_t bar, uint32_t parity, volatile int* abort_flag,
+                                          int* gerr) {
+  const unsigned long long t0 = global_ns();
+  for (uint32_t i = 0;; ++i) {
+    const bool done = mbar_try(bar, parity);
+    if (__all_sync(0xffffffffu, done)) return true;
+    if ((i & 63) == 63) {
+      int give_up = 0;
+      if ((threadIdx.x & 31) == 0) {
+        if (*abort_flag) {
+          give_up = 1;
+        } else if (global_ns() - t0 > TC_WAIT_NS) {
+          *abort_flag = 1;
+          atomicExch(gerr, kErrTimeout);
+          give_up = 1;
+        }
+      }
+      if (__shfl_sync(0xffffffffu, give_up, 0)) return false;
+    }
+  }
+}
+
+// Bounded wait used while shutting down: ignores the abort flag so that
+// copies and MMAs already in flight still land before TMEM is released.
+__device__ __forceinline__ void wait_drain(uint32_t bar, uint32_t parity, int* gerr) {
+  const unsigned long long t0 = global_ns();
+  for (uint32_t i = 0;; ++i) {
+    if (mbar_try(bar, parity)) return;
+    if ((i & 63) == 63 && global_ns() - t0 > TC_WAIT_NS) {
+      atomicExch(gerr, kErrTimeout);
+      return;
+    }
+  }
+}
+
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar,
+                                            int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4}], [%2];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms of
+// 1024 bytes (stride byte offset), sm_100 descriptor version 1.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;              // leading byte offset (unused for SW128 K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;    // stride byte offset
+  d |= (uint64_t)1 << 46;              // descriptor version
+  d |= (uint64_t)2 << 61;              // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor, kind::f16: D F32, A and B BF16, both K-major,
+// M = 128, N = n.
+__device__ __forceinline__ uint32_t idesc_bf16(int n, bool negate_a) {
+  uint32_t d = (1u << 4) | (1u << 7) | (1u << 10);
+  d |= (uint32_t)(n >> 3) << 17;
+  d |= (uint32_t)(TC_ROWS >> 4) << 24;
+  if (negate_a) d |= 1u << 13;
+  return d;
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void sts128(uint32_t addr, uint4 v) {
+  asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x), "r"(v.y),
+               "r"(v.z), "r"(v.w)
+               : "memory");
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  const uint32_t a = __bfloat16_as_ushort(__float2bfloat16_rn(lo));
+  const uint32_t b = __bfloat16_as_ushort(__float2bfloat16_rn(hi));
+  return a | (b << 16);
+}
+__device__ __forceinline__ float bf16_round(float x) {
+  return __bfloat162float(__float2bfloat16_rn(x));
+}
+
+// ------------------------------------------------------------- the kernel --
+struct ItemInfo {
+  int g, k, tl, f, sl;
+  int s0, s1, nst;
+};
+
+__device__ __forceinline__ bool decode_item(const TcParams& p, long long it, ItemInfo& d) {
+  d.g = (int)(it % p.ngroups);
+  const long long rest = it / p.ngroups;
+  d.k = (int)(rest % p.nchunk);
+  d.sl = (int)(rest / p.nchunk);
+  d.tl = d.sl / p.nf;
+  d.f = d.sl % p.nf;
+  const int cnt = __ldg(p.counts + d.tl);
+  d.s0 = d.k * p.chunk;
+  if (d.s0 >= cnt) return false;
+  d.s1 = min(d.s0 + p.chunk, cnt);
+  d.nst = (d.s1 - d.s0 + TC_KS - 1) / TC_KS;
+  return true;
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  const int NS = p.nstages;
+  const uint32_t op_base = smem_u32(smem);
+  const uint32_t stage_bytes = (uint32_t)p.max_slots * TC_SLOT;
+  uint8_t* rec_smem = smem + (size_t)NS * stage_bytes;
+  const uint32_t rec_base = smem_u32(rec_smem);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(rec_smem + (size_t)NS * TC_REC);
+  const uint32_t bar0 = smem_u32(bars);
+  // barrier addresses
+  auto rec_full = [&](int s) { return bar0 + 8u * s; };
+  auto smem_full = [&](int s) { return bar0 + 8u * (NS + s); };
+  auto smem_empty = [&](int s) { return bar0 + 8u * (2 * NS + s); };
+  const uint32_t acc_full = bar0 + 8u * (3 * NS);
+  const uint32_t acc_empty = acc_full + 8;
+  const uint32_t drain = acc_full + 16;
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 3 * NS + 3);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NS; ++s) {
+      mbar_init(rec_full(s), 1);
+      mbar_init(smem_full(s), TC_GEN_THREADS);
+      mbar_init(smem_empty(s), 1);
+    }
+    mbar_init(acc_full, 1);
+    mbar_init(acc_empty, TC_GEN_THREADS);
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == TC_MMA_WARP) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_holder)),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_holder;
+
+  if (warp < TC_GEN_WARPS) {
+    // ------------------------------------------------ phasor generators --
+    const int tid = threadIdx.x;
+    uint32_t gs = 0, ic = 0;
+    ItemInfo d;
+    for (long long it = blockIdx.x; it < p.total_items; it += gridDim.x) {
+      if (!decode_item(p, it, d)) continue;
+      const TcGroup grp = p.groups[d.g];
+      const Ucoef32* Us = p.U + (size_t)d.sl * p.Np;
+      const float* beam = p.beamT + (size_t)d.f * p.PP * p.Np;
+      const int nunits = grp.nslots * TC_ROWS * 4;
+      bool ok = true;
+      for (int j = 0; j < d.nst && ok; ++j, ++gs) {
+        const int s = (int)(gs % NS);
+        const uint32_t par = (gs / NS) & 1;
+        if (!wait_warp(rec_full(s), par, abort_flag, p.err)) { ok = false; break; }
+        if (!wait_warp(smem_empty(s), par ^ 1, abort_flag, p.err)) { ok = false; break; }
+        const SrcRec32* recs = reinterpret_cast<const SrcRec32*>(rec_smem + (size_t)s * TC_REC);
+        const uint32_t stage_op = op_base + (uint32_t)s * stage_bytes;
+        const int src0 = d.s0 + j * TC_KS;
+        for (int u = tid; u < nunits; u += TC_GEN_THREADS) {
+          const int row = u & (TC_ROWS - 1);
+          const int slot = (u >> 7) % grp.nslots;
+          const int sg = (u >> 7) / grp.nslots;
+          const int r8 = row & 7;
+          const uint32_t rowoff = (uint32_t)(row >> 3) * 1024u + (uint32_t)r8 * 128u;
+          const int h = sg >> 1, sub = sg & 1;
+          const uint32_t off_re = rowoff + ((uint32_t)((4 * h + sub) ^ r8) << 4);
+          const uint32_t off_im = rowoff + ((uint32_t)((4 * h + 2 + sub) ^ r8) << 4);
+          const uint32_t hi_tile = stage_op + (uint32_t)slot * TC_SLOT;
+          const uint32_t lo_tile = hi_tile + TC_HALF;
+          uint4 re_h = make_uint4(0, 0, 0, 0), im_h = re_h, re_l = re_h, im_l = re_h;
+          if (row < grp.slot_rows[slot]) {
+            const int a = grp.slot_block[slot] * TC_ROWS + row;
+            const Ucoef32 uc = Us[a];
+            float rv[8], iv[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              const SrcRec32 r = recs[sg * 8 + q];
+              float re = 0.f, im = 0.f;
+              if (src0 + sg * 8 + q < d.s1) {
+                const float A = beam_bilinear<float>(beam, p.Np, a, r, p.dx, p.dy);
+                const float ph = phase_cycles32(uc, r.sx, r.sy, r.sz);
+                float sn, cs;
+                sincospif(2.0f * ph, &sn, &cs);
+                const float amp = A * r.amp;
+                re = amp * cs;
+                im = amp * sn;
+              }
+              rv[q] = re;
+              iv[q] = im;
+            }
+            float rl[8], il[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              rl[q] = rv[q] - bf16_round(rv[q]);
+              il[q] = iv[q] - bf16_round(iv[q]);
+            }
+            re_h = make_uint4(pack_bf16(rv[0], rv[1]), pack_bf16(rv[2], rv[3]),
+                              pack_bf16(rv[4], rv[5]), pack_bf16(rv[6], rv[7]));
+            im_h = make_uint4(pack_bf16(iv[0], iv[1]), pack_bf16(iv[2], iv[3]),
+                              pack_bf16(iv[4], iv[5]), pack_bf16(iv[6], iv[7]));
+            re_l = make_uint4(pack_bf16(rl[0], rl[1]), pack_bf16(rl[2], rl[3]),
+                              pack_bf16(rl[4], rl[5]), pack_bf16(rl[6], rl[7]));
+            im_l = make_uint4(pack_bf16(il[0], il[1]), pack_bf16(il[2], il[3]),
+                              pack_bf16(il[4], il[5]), pack_bf16(il[6], il[7]));
+          }
+          sts128(hi_tile + off_re, re_h);
+          sts128(hi_tile + off_im, im_h);
+          sts128(lo_tile + off_re, re_l);
+          sts128(lo_tile + off_im, im_l);
+        }
+        fence_async_smem();
+        mbar_arrive(smem_full(s));
+      }
+      if (!ok) break;
+      // ------------------------------------------------------- epilogue --
+      if (!wait_warp(acc_full, ic & 1, abort_flag, p.err)) break;
+      tc_fence_after();
+      {
+        const int q = warp & 3, cb = warp >> 2;  // lane quadrant, 128-column block
+        const int pr = cb >> 1, plane = cb & 1;
+        if (pr < grp.npairs) {
+          const int I = grp.pI[pr], J = grp.pJ[pr];
+          float* out = p.partial +
+                       (((size_t)d.sl * p.nchunk + d.k) * 2 + plane) * (size_t)p.Np * p.Np;
+          const int a = I * TC_ROWS + q * 32 + lane;
+#pragma unroll 1
+          for (int c32 = 0; c32 < 4; ++c32) {
+            float v[32];
+            tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cb * 128 + c32 * 32), v);
+            const int b0 = J * TC_ROWS + c32 * 32;
+#pragma unroll
+            for (int c = 0; c < 32; ++c) out[(size_t)(b0 + c) * p.Np + a] = v[c];
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(acc_empty);
+      ++ic;
+    }
+  } else if (warp == TC_PRODUCER_WARP) {
+    // ----------------------------------------------------- TMA producer --
+    if (lane == 0) {
+      uint32_t gs = 0;
+      ItemInfo d;
+      bool ok = true;
+      for (long long it = blockIdx.x; it < p.total_items && ok; it += gridDim.x) {
+        if (!decode_item(p, it, d)) continue;
+        for (int j = 0; j < d.nst; ++j, ++gs) {
+          const int s = (int)(gs % NS);
+          const uint32_t par = (gs / NS) & 1;
+          // the generators have finished with the previous round of this slot
+          if (!wait1(smem_full(s), par ^ 1, abort_flag, p.err)) { ok = false; break; }
+          mbar_expect_tx(rec_full(s), TC_REC);
+          tma_load_2d(rec_base + (uint32_t)s * TC_REC, &rec_map, rec_full(s), 0,
+                      d.tl * p.nsrc + d.s0 + j * TC_KS);
+        }
+      }
+      // let the copies still in flight land before the CTA can exit
+      const uint32_t first = gs > (uint32_t)NS ? gs - NS : 0;
+      for (uint32_t g = first; g < gs; ++g) wait_drain(rec_full((int)(g % NS)), (g / NS) & 1, p.err);
+    }
+  } else {
+    // ------------------------------------------------------- MMA issuer --
+    if (lane == 0) {
+      uint32_t gs = 0, ic = 0;
+      ItemInfo d;
+      bool ok = true;
+      for (long long it = blockIdx.x; it < p.total_items && ok; it += gridDim.x) {
+        if (!decode_item(p, it, d)) continue;
+        const TcGroup grp = p.groups[d.g];
+        uint32_t idp[2], idn[2];
+        for (int q = 0; q < grp.npairs; ++q) {
+          idp[q] = idesc_bf16(grp.pN[q], false);
+          idn[q] = idesc_bf16(grp.pN[q], true);
+        }
+        if (!wait1(acc_empty, (ic & 1) ^ 1, abort_flag, p.err)) { ok = false; break; }
+        tc_fence_after();
+        for (int j = 0; j < d.nst; ++j, ++gs) {
+          const int s = (int)(gs % NS);
+          const uint32_t par = (gs / NS) & 1;
+          if (!wait1(smem_full(s), par, abort_flag, p.err)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t stage_op = op_base + (uint32_t)s * stage_bytes;
+          for (int q = 0; q < grp.npairs; ++q) {
+            const uint32_t a_hi = stage_op + (uint32_t)grp.pa[q] * TC_SLOT;
+            const uint32_t b_hi = stage_op + (uint32_t)grp.pb[q] * TC_SLOT;
+            const uint32_t A[2] = {a_hi, a_hi + TC_HALF};
+            const uint32_t B[2] = {b_hi, b_hi + TC_HALF};
+            const uint32_t d_re = tmem + (uint32_t)(q * 256);
+            const uint32_t d_im = d_re + 128;
+            // products (hi, hi), (hi, lo), (lo, hi)
+            const int pa_[3] = {0, 0, 1}, pb_[3] = {0, 1, 0};
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const uint32_t kre = (uint32_t)(2 * h) * 32u, kim = (uint32_t)(2 * h + 1) * 32u;
+#pragma unroll
+              for (int pr = 0; pr < 3; ++pr) {
+                const uint32_t first = (j == 0 && h == 0 && pr == 0) ? 0u : 1u;
+                const uint32_t a = A[pa_[pr]], b = B[pb_[pr]];
+                mma_bf16(d_re, sw128_desc(a + kre), sw128_desc(b + kre), idp[q], first);
+                mma_bf16(d_re, sw128_desc(a + kim), sw128_desc(b + kim), idp[q], 1u);
+                mma_bf16(d_im, sw128_desc(a + kim), sw128_desc(b + kre), idp[q], first);
+                mma_bf16(d_im, sw128_desc(a + kre), sw128_desc(b + kim), idn[q], 1u);
+              }
+            }
+          }
+          mma_commit(smem_empty(s));
+        }
+        if (!ok) break;
+        mma_commit(acc_full);
+        ++ic;
+      }
+      // every MMA issued by this thread completes before TMEM is released
+      mma_commit(drain);
+      wait_drain(drain, 0, p.err);
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == TC_MMA_WARP) {
+    __syncwarp();
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+  }
+}
+
+// ------------------------------------------------------------------- host --
+namespace {
+
+std::vector<TcGroup> make_groups(int nant) {
+  const int nb = ceil_div(nant, TC_ROWS);
+  auto rows_of = [&](int blk) { return std::min(TC_ROWS, nant - blk * TC_ROWS); };
+  auto ncols = [&](int blk) { return ((rows_of(blk) + 15) / 16) * 16; };
+  std::vector<std::vector<std::pair<int, int>>> raw;
+  std::vector<std::pair<int, int>> singles;
+  for (int I = 0; I < nb; ++I) {
+    int J = I;
+    for (; J + 1 < nb; J += 2) raw.push_back({{I, J}, {I, J + 1}});
+    if (J < nb) singles.push_back({I, J});
+  }
+  // merge single pairs when the two touch at most three blocks
+  std::vector<bool> used(singles.size(), false);
+  for (size_t i = 0; i < singles.size(); ++i) {
+    if (used[i]) continue;
+    used[i] = true;
+    bool merged = false;
+    for (size_t k = i + 1; k < singles.size() && !merged; ++k) {
+      if (used[k]) continue;
+      int blocks[4] = {singles[i].first, singles[i].second, singles[k].first, singles[k].second};
+      std::sort(blocks, blocks + 4);
+      const int distinct = (int)(std::unique(blocks, blocks + 4) - blocks);
+      if (distinct <= 3) {
+        raw.push_back({singles[k], singles[i]});
+        used[k] = true;
+        merged = true;
+      }
+    }
+    if (!merged) raw.push_back({singles[i]});
+  }
+  std::vector<TcGroup> out;
+  for (auto& prs : raw) {
+    TcGroup g{};
+    g.npairs = (int)prs.size();
+    g.nslots = 0;
+    auto slot_of = [&](int blk) {
+      for (int s = 0; s < g.nslots; ++s)
+        if (g.slot_block[s] == blk) return s;
+      g.slot_block[g.nslots] = blk;
+      g.slot_rows[g.nslots] = rows_of(blk);
+      return g.nslots++;
+    };
+    for (int q = 0; q < g.npairs; ++q) {
+      g.pI[q] = prs[q].first;
+      g.pJ[q] = prs[q].second;
+      g.pa[q] = slot_of(prs[q].first);
+      g.pb[q] = slot_of(prs[q].second);
+      g.pN[q] = ncols(prs[q].second);
+    }
+    out.push_back(g);
+  }
+  return out;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* ptr = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+  }
+  return fn;
+}
+
+}  // namespace
+
+int tc_num_groups(int nant) { return (int)make_groups(nant).size(); }
+
+size_t tc_group_table_bytes(int nant) { return sizeof(TcGroup) * make_groups(nant).size(); }
+
+int tc_fill_group_table(int nant, void* host_buf) {
+  const auto g = make_groups(nant);
+  std::copy(g.begin(), g.end(), static_cast<TcGroup*>(host_buf));
+  return (int)g.size();
+}
+
+int tc_chunk_sources(int nsrc, int nslices, int ngroups, int num_sms) {
+  // enough items to fill every SM a few times, chunks of 1k-16k sources
+  const long long want = (long long)nslices * ngroups * std::max(nsrc / 2, 1) / (8LL * num_sms);
+  long long c = std::min<long long>(16384, std::max<long long>(1024, want));
+  c = (c + TC_KS - 1) / TC_KS * TC_KS;
+  return (int)c;
+}
+
+cudaError_t launch_tc(const TcLaunch& L, cudaStream_t st) {
+  if (L.nsrc <= 0 || L.nt <= 0) return cudaSuccess;
+  auto encode = encode_fn();
+  if (!encode) return cudaErrorNotSupported;
+  CUtensorMap map;
+  const cuuint64_t gdim[2] = {8, (cuuint64_t)L.nt * L.nsrc};
+  const cuuint64_t gstride[1] = {sizeof(SrcRec32)};
+  const cuuint32_t box[2] = {8, TC_KS};
+  const cuuint32_t estride[2] = {1, 1};
+  CUresult r = encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(L.rec), gdim,
+                      gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                      CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+
+  TcParams p{};
+  p.counts = L.counts;
+  p.nsrc = L.nsrc;
+  p.nt = L.nt;
+  p.nf = L.nf;
+  p.U = static_cast<const Ucoef32*>(L.U);
+  p.beamT = L.beamT;
+  p.Np = L.Np;
+  p.nant = L.nant;
+  p.PP = L.P * L.P;
+  p.dx = L.P > 1 ? 1 : 0;
+  p.dy = L.P > 1 ? L.P : 0;
+  p.partial = L.partial;
+  p.chunk = L.chunk;
+  p.nchunk = ceil_div(L.nsrc, L.chunk);
+  p.groups = static_cast<const TcGroup*>(L.groups);
+  p.ngroups = L.ngroups;
+  p.max_slots = L.max_slots;
+  p.err = L.err;
+  p.total_items = (long long)L.nt * L.nf * p.nchunk * p.ngroups;
+  const int per_stage = p.max_slots * TC_SLOT + TC_REC;
+  const int fixed = 1024 /*alignment*/ + 512 /*barriers, holder*/;
+  p.nstages = std::min(4, (TC_SMEM_LIMIT - fixed) / per_stage);
+  if (p.nstages < 2) return cudaErrorInvalidConfiguration;
+  const int smem = fixed + p.nstages * per_stage;
+  cudaError_t e = cudaFuncSetAttribute(tc_vis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       smem);
+  if (e != cudaSuccess) return e;
+  const long long grid = std::min<long long>(L.num_sms, p.total_items);
+  tc_vis_kernel<<<(int)grid, TC_THREADS, smem, st>>>(map, p);
+  return cudaGetLastError();
+}
+
+size_t tc_partial_floats(int Np, int nsrc, int nslices, int chunk) {
+  return (size_t)nslices * ceil_div(std::max(nsrc, 1), chunk) * 2 * (size_t)Np * Np;
+}
+
+int tc_max_slots(int nant) {
+  int m = 1;
+  for (auto& g : make_groups(nant)) m = std::max(m, g.nslots);
+  return m;
+}
+
+}  // namespace hv

@@ -1,0 +1,119 @@
+/*
+ * heravis.h -- C ABI of the GB300 visibility simulator (libheravis.so).
+ *
+ * The library is a drop-in for the one hot path of hera_gpu,
+ * hera_gpu.vis.vis_gpu (reference hera_gpu/vis.py:144-262): per time, rotate
+ * sources to topocentric, drop those below the horizon, bilinearly
+ * interpolate each antenna's beam, form v[a,s] = A_a(l,m) sqrt(I_s)
+ * exp(2 pi i nu tau_as) and return V[a,b] = sum_s v[a,s] conj(v[b,s]) as the
+ * full Hermitian (ntimes, nant, nant) matrix.
+ *
+ * The reference exposes that path as a Python function only; these entry
+ * points are what a foreign-function binding of it binds (the ctypes binding
+ * shipped in hera_gpu_gb300/_native.py, and the stubs in INTEGRATION.md).
+ *
+ * Conventions
+ *  - Every call returns an hv_status; hv_last_error() gives the message of the
+ *    last failure on that context.  Bad shapes or arguments return
+ *    HV_ERR_ARG (the reference raises AssertionError, vis.py:147,161-169).
+ *  - precision 1: float32 inputs, complex64 output (interleaved re, im);
+ *    precision 2: float64 inputs, complex128 output (vis.py:147-157).
+ *  - Array layouts are C order, exactly as the reference's arguments:
+ *      antpos  (nant, 3)            metres
+ *      eq2tops (ntimes, 3, 3)       equatorial -> topocentric rotations
+ *      crd_eq  (3, nsrc)            equatorial unit vectors
+ *      I_sky   (nsrc,)              intensities (sqrt taken internally)
+ *      bm_cube (nant, P, P)         beam on the grid linspace(-1,1,P),
+ *                                   axis order [ant, y(m), x(l)]
+ *      vis     (ntimes, nant, nant) output
+ *    Multi-frequency calls take bm_cubes (nfreq, nant, P, P) and write
+ *    vis (nfreq, ntimes, nant, nant).
+ *  - A context owns one CUDA stream and a workspace on one device; it is not
+ *    thread-safe (one thread per context, or a lock around it).
+ */
+#ifndef HERAVIS_H
+#define HERAVIS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  HV_OK = 0,
+  HV_ERR_ARG = 1,         /* bad shape / argument (reference: AssertionError) */
+  HV_ERR_OOM = 2,         /* device allocation failed or HBM budget exceeded  */
+  HV_ERR_CUDA = 3,        /* CUDA runtime error                               */
+  HV_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up               */
+  HV_ERR_UNSUPPORTED = 5  /* no suitable GPU / method unavailable             */
+} hv_status;
+
+typedef enum {
+  HV_METHOD_AUTO = 0,     /* tensor-core form for precision 1, FP64 for 2      */
+  HV_METHOD_PLAIN = 1,    /* the reference's method: phasors to HBM, then an
+                             FP32 (precision 1) / FP64 (precision 2) SIMT
+                             Hermitian product                                 */
+  HV_METHOD_TC_BF16 = 2   /* fused: phasors generated in shared memory, split
+                             BF16 tcgen05 products, FP32 accumulation in TMEM  */
+} hv_method;
+
+typedef struct hv_context hv_context;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int hv_version(void);
+
+/* Open a context on CUDA device `device`; `hbm_budget_bytes` caps the
+ * workspace the context may hold (0 = no cap).  Replaces the import-time
+ * pycuda.autoinit context of the reference (vis.py:1). */
+int hv_create(hv_context** ctx, int device, size_t hbm_budget_bytes);
+int hv_destroy(hv_context* ctx);
+const char* hv_last_error(const hv_context* ctx);
+
+/* Kernel launches issued by this context since creation (all methods). */
+uint64_t hv_launch_count(const hv_context* ctx);
+
+/* Drop-in for vis_gpu(antpos, freq, eq2tops, crd_eq, I_sky, bm_cube,
+ * precision=...) (reference hera_gpu/vis.py:144-146).  Host buffers in and
+ * out; returns when `vis_out` is written.  `freq` in Hz. */
+int hv_vis_gpu(hv_context* ctx, int precision, int method,
+               const void* antpos, int nant, double freq,
+               const void* eq2tops, int ntimes,
+               const void* crd_eq, const void* I_sky, int nsrc,
+               const void* bm_cube, int beam_px, void* vis_out);
+
+/* Several frequencies in one call (the reference loops vis_gpu once per
+ * frequency, each call with that frequency's beam cube, vis.py:144).
+ * freqs: host array (nfreq,) Hz.  Host buffers in and out. */
+int hv_vis_multifreq(hv_context* ctx, int precision, int method,
+                     const void* antpos, int nant,
+                     const double* freqs, int nfreq,
+                     const void* eq2tops, int ntimes,
+                     const void* crd_eq, const void* I_sky, int nsrc,
+                     const void* bm_cubes, int beam_px, void* vis_out);
+
+/* As hv_vis_multifreq with every array already in device memory (freqs
+ * stays a host array).  Work is ordered on `stream` (a cudaStream_t; NULL =
+ * the context's stream) and the call returns without synchronising; call
+ * hv_sync() before reading `d_vis_out` on another stream or the host. */
+int hv_vis_multifreq_device(hv_context* ctx, int precision, int method,
+                            const void* d_antpos, int nant,
+                            const double* freqs, int nfreq,
+                            const void* d_eq2tops, int ntimes,
+                            const void* d_crd_eq, const void* d_I_sky, int nsrc,
+                            const void* d_bm_cubes, int beam_px,
+                            void* d_vis_out, void* stream);
+
+/* Wait for the context's work and report any deferred device-side error
+ * (e.g. HV_ERR_TIMEOUT from a bounded wait). */
+int hv_sync(hv_context* ctx);
+
+/* Page-locked host memory for fast host<->device copies (cudaHostAlloc). */
+int hv_host_alloc(hv_context* ctx, size_t bytes, void** ptr);
+int hv_host_free(hv_context* ctx, void* ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HERAVIS_H */

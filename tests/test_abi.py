@@ -1,0 +1,79 @@
+"""The C ABI library: it loads, exports every declared entry point, and the
+Python host layer checks shapes like the reference -- all without a GPU."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from hera_gpu_gb300 import _native, vis_gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", h)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            names |= set(re.findall(r"\b(hv_[a-z0-9_]+)\s*\(", text))
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(_native.LIB_PATH):
+        from hera_gpu_gb300 import build
+        build.build()
+    return _native.load_library()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = declared_symbols()
+    assert {"hv_create", "hv_destroy", "hv_vis_gpu", "hv_vis_multifreq",
+            "hv_vis_multifreq_device", "hv_last_error", "hv_sync"} <= names
+    out = subprocess.run(["nm", "-D", "--defined-only", _native.LIB_PATH],
+                         capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (hv_[a-z0-9_]+)", out))
+    assert names <= exported, names - exported
+    for n in names:
+        assert hasattr(lib, n)
+    assert set(_native.SIGNATURES) == names
+
+
+def test_version(lib):
+    assert lib.hv_version() >= 10000
+
+
+def test_create_without_gpu_fails_loudly(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(_native.HeraVisError):
+        _native.Context(0)
+
+
+NANT, NTIMES, BM_PIX, NPIX = 16, 10, 31, 12 * 16 ** 2
+
+
+@pytest.mark.parametrize("bad", ["antpos", "eq2tops", "crd_eq", "bm_cube", "I_sky"])
+def test_shape_asserts_before_any_device_work(bad):
+    # test_vis_gpu.py:172-191 of the reference: transposed inputs raise AssertionError
+    args = dict(antpos=np.zeros((NANT, 3)), eq2tops=np.zeros((NTIMES, 3, 3)),
+                crd_eq=np.zeros((3, NPIX)), I_sky=np.zeros(NPIX),
+                bm_cube=np.zeros((NANT, BM_PIX, BM_PIX)))
+    if bad == "I_sky":
+        args[bad] = np.zeros((NPIX, 1))
+    else:
+        args[bad] = args[bad].T
+    with pytest.raises(AssertionError):
+        vis_gpu(args["antpos"], 0.15, args["eq2tops"], args["crd_eq"], args["I_sky"],
+                args["bm_cube"])
+
+
+def test_precision_must_be_1_or_2():
+    with pytest.raises(AssertionError):
+        vis_gpu(np.zeros((2, 3)), 0.15, np.zeros((1, 3, 3)), np.zeros((3, 4)), np.zeros(4),
+                np.zeros((2, 3, 3)), precision=3)
