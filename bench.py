@@ -1,0 +1,478 @@
+"""Throughput of the visibility simulator on GB300 (one JSON line on rank 0).
+
+Workload (the precision-form configuration): 350 antennas on a 14.6 m hex
+grid, 1,048,576 sphere-uniform power-law sources, 64 channels evenly spaced
+on 100-200 MHz with per-channel 350x63x63 Airy beam cubes, LSTs over one
+hour at latitude -30.72 deg; seeded synthetic data.  One step = one call of
+the hot path over 4 consecutive LSTs (of 120) and all 64 channels, i.e.
+4 * 64 * 350**2 visibilities.
+
+Arms
+  (default)          fused tensor-core form through the C ABI, inputs resident
+                     in HBM (``value``); the same call through the public
+                     Python API with page-locked host buffers, copies inside
+                     the timed region (``e2e``); the plain FP32 form on one
+                     step for comparison; the CPU oracle port on a bounded
+                     sample (``cpu_baseline``).
+  --impl reference   the reference's CPU algorithm (the oracle port of
+                     hera_gpu/tests/test_vis_gpu.py:278-357) on the host
+                     cores, on a bounded sample of the same workload.
+
+Several GPUs run independent replicas (the path has no exchange step).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NANT, NSRC, NFREQ, NTIMES, BEAM_PX = 350, 1_048_576, 64, 120, 63
+T_PER_STEP = 4
+FMIN, FMAX = 100e6, 200e6
+CPU_SAMPLE_SRC = 16384          # sources per host process per CPU sample
+CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nsrc", type=int, default=NSRC)
+    ap.add_argument("--nfreq", type=int, default=NFREQ)
+    ap.add_argument("--nant", type=int, default=NANT)
+    ap.add_argument("--method", default="tc", choices=["tc", "plain"])
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------- workload --
+def make_workload(nant, nsrc, nfreq, seed=0):
+    import numpy as np
+    from hera_gpu_gb300 import synth
+    cfg = synth.config_array(seed=seed, nant=nant, nsrc=nsrc, ntimes=NTIMES, nfreq=nfreq,
+                             fmin=FMIN, fmax=FMAX, P=BEAM_PX)
+    w = dict(antpos=cfg["antpos"].astype(np.float32), freqs=cfg["freqs"],
+             eq2tops=cfg["eq2tops"].astype(np.float32), crd_eq=cfg["crd_eq"].astype(np.float32),
+             I_sky=cfg["I_sky"].astype(np.float32))
+    w["bm_cubes"] = synth.beams_for(cfg, dtype=np.float32)
+    return w
+
+
+def sources_up(w, t):
+    """Sources above the horizon at time t (FP64, as the prep kernel)."""
+    import numpy as np
+    z = np.asarray(w["eq2tops"][t], dtype=np.float64)[2] @ np.asarray(w["crd_eq"], dtype=np.float64)
+    return int(np.count_nonzero(z > 0))
+
+
+def tc_chunk(nsrc, nslices, ngroups, num_sms):
+    """Split-K chunk the library picks (hv_tc.cu tc_chunk_sources)."""
+    want = nslices * ngroups * max(nsrc // 2, 1) // (8 * num_sms)
+    c = min(16384, max(1024, want))
+    return (c + 31) // 32 * 32
+
+
+def tc_pairs_ncols(nant):
+    """Sum over antenna-block pairs I <= J of the MMA N of the pair."""
+    nb = (nant + 127) // 128
+    tot = 0
+    for I in range(nb):
+        for J in range(I, nb):
+            tot += (min(128, nant - 128 * J) + 15) // 16 * 16
+    return tot
+
+
+def tc_num_groups(nant):
+    nb = (nant + 127) // 128
+    pairs_rows = [[(I, J) for J in range(I, nb)] for I in range(nb)]
+    groups, singles = 0, []
+    for row in pairs_rows:
+        groups += len(row) // 2
+        if len(row) % 2:
+            singles.append(row[-1])
+    used = [False] * len(singles)
+    for i in range(len(singles)):
+        if used[i]:
+            continue
+        used[i] = True
+        for k in range(i + 1, len(singles)):
+            if not used[k] and len({*singles[i], *singles[k]}) <= 3:
+                used[k] = True
+                break
+        groups += 1
+    return groups
+
+
+# ------------------------------------------------------------------- clocks --
+class ClockSampler:
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={CLOCK_FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            lines = open(self.path).read().strip().splitlines()
+        except OSError:
+            lines = []
+        for ln in lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if self.path:
+            os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# -------------------------------------------------------------- CPU oracle --
+def _cpu_worker(args):
+    """One host process: the oracle port on one block of sources (checker and
+    CPU baseline only)."""
+    import numpy as np
+    from oracle import vis_oracle_partial
+    antpos, freq, eq2top, crd, I, bm = args
+    t0 = time.perf_counter()
+    V = vis_oracle_partial(antpos, freq, eq2top, crd, I, bm.astype(np.float64), 0, crd.shape[1],
+                           dtype=np.float64)
+    return V, time.perf_counter() - t0
+
+
+def cpu_pool():
+    """One single-threaded oracle process per host core (spawned, so it is
+    safe before or after CUDA initialisation)."""
+    import multiprocessing as mp
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    for k in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[k] = "1"
+    return mp.get_context("spawn").Pool(cores), cores
+
+
+def cpu_sample(pool, cores, w, t, f):
+    """Oracle on cores x CPU_SAMPLE_SRC sources of slice (t, f), one block of
+    sources per process; returns (V of the sample, seconds, sources).  The
+    seconds are the longest per-process compute time (the parallel span,
+    without the inter-process transfer of inputs)."""
+    import numpy as np
+    nsamp = min(cores * CPU_SAMPLE_SRC, w["crd_eq"].shape[1])
+    bounds = np.linspace(0, nsamp, cores + 1).astype(int)
+    a64 = lambda x: np.asarray(x, dtype=np.float64)
+    jobs = [(a64(w["antpos"]), float(w["freqs"][f]), a64(w["eq2tops"][t]),
+             a64(w["crd_eq"][:, bounds[i]:bounds[i + 1]]), a64(w["I_sky"][bounds[i]:bounds[i + 1]]),
+             np.asarray(w["bm_cubes"][f])) for i in range(cores)]
+    parts = pool.map(_cpu_worker, jobs)
+    span = max(p[1] for p in parts)
+    return sum(p[0] for p in parts), span, nsamp
+
+
+def cpu_rate(wall, nsamp, nant, nsrc_full):
+    """vis/s of the CPU path on a full slice, extrapolated linearly in sources."""
+    t_slice = wall * nsrc_full / nsamp
+    return nant * nant / t_slice
+
+
+# ------------------------------------------------------------------ ranks --
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    import numpy as np
+    pool, cores = cpu_pool()
+    w = make_workload(args.nant, args.nsrc, args.nfreq)
+    rates = []
+    for i in range(args.warmup + args.steps):
+        t = (i * T_PER_STEP) % NTIMES
+        _, wall, nsamp = cpu_sample(pool, cores, w, t, i % args.nfreq)
+        if i >= args.warmup:
+            rates.append(cpu_rate(wall, nsamp, args.nant, args.nsrc))
+    pool.close()
+    value = float(np.mean(rates))
+    sample = (f"{cores} host processes x {CPU_SAMPLE_SRC} sources of one (time, channel) slice "
+              f"per step, extrapolated linearly to {args.nsrc} sources")
+    line = {
+        "impl": "reference", "metric": "visibilities/s", "value": value, "unit": "vis/s",
+        "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * T_PER_STEP * args.nfreq * args.nant ** 2 / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": f"{args.nant} ant x {args.nsrc} src x {args.nfreq} ch, "
+                               f"{T_PER_STEP} LSTs per step", "nant": args.nant,
+                   "nsrc": args.nsrc, "nfreq": args.nfreq},
+        "cpu_baseline": {"value": value, "unit": "vis/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "vis/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def load_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def load_traffic():
+    """DRAM bytes per (slice x source above the horizon) of the fused kernel,
+    from the committed ncu summary (None if absent)."""
+    path = os.path.join(ROOT, "profiles", "tc_vis_kernel.md")
+    try:
+        for ln in open(path):
+            if ln.startswith("dram_bytes_per_slice_source:"):
+                return float(ln.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def run_ours(args):
+    import numpy as np
+    world, rank, local = dist_setup()
+    pool = cores = None
+    if rank == 0 and not args.no_cpu:
+        pool, cores = cpu_pool()      # spawned before the first CUDA call
+    import torch
+    from hera_gpu_gb300 import _native, vis_gpu, vis_gpu_multifreq
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    ctx = _native.Context(local)
+    num_sms = torch.cuda.get_device_properties(local).multi_processor_count
+    w = make_workload(args.nant, args.nsrc, args.nfreq, seed=rank)
+    N, S, F = args.nant, args.nsrc, args.nfreq
+    dev = torch.device("cuda", local)
+    d = {k: torch.from_numpy(np.ascontiguousarray(w[k])).to(dev)
+         for k in ("antpos", "eq2tops", "crd_eq", "I_sky", "bm_cubes")}
+    d_out = torch.empty((F, T_PER_STEP, N, N), dtype=torch.complex64, device=dev)
+    torch.cuda.synchronize(dev)
+    # a stream of our own: the library launches on it and the events time it
+    stream = torch.cuda.Stream(dev)
+
+    def step(i, method):
+        t0 = (i * T_PER_STEP) % NTIMES
+        ctx.vis_multifreq_device(1, method, d["antpos"].data_ptr(), N, w["freqs"],
+                                 d["eq2tops"][t0:t0 + T_PER_STEP].data_ptr(), T_PER_STEP,
+                                 d["crd_eq"].data_ptr(), d["I_sky"].data_ptr(), S,
+                                 d["bm_cubes"].data_ptr(), BEAM_PX, d_out.data_ptr(),
+                                 stream.cuda_stream)
+        return t0
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- device-resident throughput of the chosen form -------------------
+    for i in range(args.warmup):
+        step(i, args.method)
+    ctx.sync()
+    barrier()
+    ctx.set_profiling(True)
+    ctx.profile_read()
+    l0 = ctx.launches
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times = []
+    with ClockSampler(local) as clocks:
+        barrier()
+        ev0.record(stream)
+        for i in range(args.warmup, args.warmup + args.steps):
+            times.append(step(i, args.method))
+        ev1.record(stream)
+        barrier()
+    ms = ev0.elapsed_time(ev1)
+    ctx.sync()
+    kern_ms, kern_launches = ctx.profile_read()
+    ctx.set_profiling(False)
+    launches = ctx.launches - l0
+    if world > 1:
+        tt = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tt.item())
+    vis_per_step = T_PER_STEP * F * N * N
+    value = world * args.steps * vis_per_step / (ms / 1e3)
+    clk = clocks.summary()
+
+    # ---- roofline of the contraction kernel -------------------------------
+    peaks, peak_src = load_peaks()
+    s_up = [sources_up(w, t0 + k) for t0 in times for k in range(T_PER_STEP)]
+    herk_flops = sum(4.0 * N * (N + 1) * su * F for su in s_up)
+    if args.method == "tc":
+        ng = tc_num_groups(N)
+        chunk = tc_chunk(S, T_PER_STEP * F, ng, num_sms)
+        stages = sum(sum(math.ceil(min(chunk, su - k0) / 32) for k0 in range(0, su, chunk))
+                     for su in s_up) * F
+        hw_flops = stages * 24 * 2 * 128 * 16 * tc_pairs_ncols(N)
+        peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
+        traffic_unit = load_traffic()
+        units = sum(s_up) * F
+        roof = {"bound": "tensor", "achieved": herk_flops / (kern_ms / 1e3) / 1e12,
+                "peak": peak, "unit": "TFLOP/s",
+                "frac": herk_flops / (kern_ms / 1e3) / 1e12 / peak,
+                "traffic": (traffic_unit * units / kern_launches) if traffic_unit else None,
+                "kernel": "tc_vis_kernel", "launches": kern_launches,
+                "kernel_ms": kern_ms,
+                "hw_tflops": hw_flops / (kern_ms / 1e3) / 1e12,
+                "hw_frac": hw_flops / (kern_ms / 1e3) / 1e12 / peak,
+                "peak_kind": f"bf16 dense sustained ({peak_src})",
+                "algorithmic": "4 N (N+1) S_up flops per slice (Hermitian upper triangle); "
+                               "hw_* counts the issued split-BF16 MMAs (3 products, 128-blocks)"}
+    else:
+        peak = 152 * 128 * 2 * 1.92e9 / 1e12
+        roof = {"bound": "fp32-simt", "achieved": herk_flops / (kern_ms / 1e3) / 1e12,
+                "peak": peak, "unit": "TFLOP/s",
+                "frac": herk_flops / (kern_ms / 1e3) / 1e12 / peak, "traffic": None,
+                "kernel": "herk_plain_kernel", "launches": kern_launches, "kernel_ms": kern_ms}
+
+    line = {
+        "metric": "visibilities/s", "value": value, "unit": "vis/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16" if args.method == "tc" else "fp32",
+        "data": "synthetic (seeded); inputs larger than L2 (beam cubes "
+                f"{w['bm_cubes'].nbytes / 1e6:.0f} MB)",
+        "config": {"workload": f"{N} ant x {S} src x {F} ch (100-200 MHz), {T_PER_STEP} of "
+                               f"{NTIMES} LSTs per step, beams {BEAM_PX}x{BEAM_PX}",
+                   "nant": N, "nsrc": S, "nfreq": F, "ntimes_per_step": T_PER_STEP,
+                   "method": args.method, "l2": "inputs larger than L2",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": roof, "clocks": clk, "gpu_launches": launches,
+    }
+
+    # ---- end to end through the public API, host buffers -----------------
+    if not args.no_e2e:
+        pin = {k: ctx.pinned_empty(w[k].shape, w[k].dtype) for k in
+               ("antpos", "crd_eq", "I_sky", "bm_cubes")}
+        for k in pin:
+            pin[k][...] = w[k]
+        e2t = ctx.pinned_empty((T_PER_STEP, 3, 3), np.float32)
+        out = ctx.pinned_empty((F, T_PER_STEP, N, N), np.complex64)
+
+        def e2e_step(i):
+            t0 = (i * T_PER_STEP) % NTIMES
+            e2t[...] = w["eq2tops"][t0:t0 + T_PER_STEP]
+            vis_gpu_multifreq(pin["antpos"], w["freqs"], e2t, pin["crd_eq"], pin["I_sky"],
+                              pin["bm_cubes"], precision=1, method=args.method, context=ctx,
+                              out=out)
+            return float(out[0, 0, 0, 0].real)   # read of the step's result
+        e2e_step(0)
+        barrier()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            e2e_step(i)
+        e2e_s = time.perf_counter() - t0
+        h2d = sum(pin[k].nbytes for k in pin) + e2t.nbytes + 8 * F
+        line["e2e"] = {"value": world * args.steps * vis_per_step / e2e_s, "unit": "vis/s",
+                       "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(out.nbytes),
+                       "api": "hera_gpu_gb300.vis_gpu_multifreq -> hv_vis_multifreq"}
+
+    # ---- the plain FP32 form on one step (the method of the reference) ----
+    if rank == 0 and not args.no_plain and args.method == "tc":
+        step(0, "plain")
+        ctx.sync()
+        ctx.set_profiling(True)
+        ctx.profile_read()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step(1, "plain")
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        pms = e0.elapsed_time(e1)
+        pk_ms, _ = ctx.profile_read()
+        ctx.set_profiling(False)
+        pflops = sum(4.0 * N * (N + 1) * sources_up(w, T_PER_STEP + k) * F
+                     for k in range(T_PER_STEP))
+        line["plain_fp32"] = {"value": vis_per_step / (pms / 1e3), "unit": "vis/s",
+                              "ms_per_step": pms,
+                              "herk_tflops": pflops / (pk_ms / 1e3) / 1e12,
+                              "tc_speedup": value / world / (vis_per_step / (pms / 1e3))}
+
+    # ---- CPU baseline on a bounded sample, and the error of that sample ----
+    if rank == 0 and pool is not None:
+        V_cpu, wall, nsamp = cpu_sample(pool, cores, w, 0, 0)
+        pool.close()
+        line["cpu_baseline"] = {
+            "value": cpu_rate(wall, nsamp, N, S), "unit": "vis/s", "cores": cores,
+            "kind": "port",
+            "sample": f"{nsamp} sources of slice (t=0, {w['freqs'][0] / 1e6:.0f} MHz) on {cores} "
+                      f"processes, extrapolated linearly to {S} sources"}
+        errs = {}
+        for method in ("tc", "plain"):
+            v = vis_gpu(w["antpos"], float(w["freqs"][0]), w["eq2tops"][:1],
+                        w["crd_eq"][:, :nsamp], w["I_sky"][:nsamp], w["bm_cubes"][0],
+                        precision=1, method=method, context=ctx)[0]
+            errs[method] = float(np.linalg.norm(v - V_cpu) / np.linalg.norm(V_cpu))
+        line["rel_err_vs_fp64"] = {**errs, "sample": f"{N} ant x {nsamp} src, one slice"}
+
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -40,6 +40,8 @@ SIGNATURES = {
                                          _PTR, _c_int, _PTR, _PTR, _c_int, _PTR, _c_int, _PTR,
                                          _c_void_p]),
     "hv_sync": (_c_int, [_c_void_p]),
+    "hv_set_profiling": (_c_int, [_c_void_p, _c_int]),
+    "hv_profile_read": (_c_int, [_c_void_p, ctypes.POINTER(_c_double), ctypes.POINTER(ctypes.c_uint64)]),
     "hv_host_alloc": (_c_int, [_c_void_p, _c_size_t, ctypes.POINTER(_c_void_p)]),
     "hv_host_free": (_c_int, [_c_void_p, _c_void_p]),
 }
@@ -152,6 +154,17 @@ class Context:
             ctypes.c_void_p(d_bm_cubes), int(beam_px), ctypes.c_void_p(d_out),
             ctypes.c_void_p(stream))
         self.check(rc)
+
+    def set_profiling(self, enable: bool):
+        self.check(self.lib.hv_set_profiling(self.h, 1 if enable else 0))
+
+    def profile_read(self):
+        """(milliseconds, launches) of the visibility-product kernels since
+        the last read (CUDA events on their stream)."""
+        ms = ctypes.c_double()
+        n = ctypes.c_uint64()
+        self.check(self.lib.hv_profile_read(self.h, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, int(n.value)
 
     def pinned_empty(self, shape, dtype):
         """A numpy array in page-locked host memory, freed when the last view

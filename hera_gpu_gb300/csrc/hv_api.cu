@@ -17,8 +17,10 @@
 #include <algorithm>
 #include <cstring>
 #include <string>
+#include <utility>
+#include <vector>
 
-#include "../../include/heravis.h"
+#include "heravis.h"
 #include "hv_internal.cuh"
 #include "hv_kernels.h"
 
@@ -41,10 +43,14 @@ struct hv_context {
   std::string err;
   uint64_t launches = 0;
   int* d_err = nullptr;  // device-side error flag (bounded waits)
+  // profiling of the visibility-product kernels
+  bool profiling = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
   // staging of host-API inputs / outputs
   DevBuf in_antpos, in_eq2tops, in_crd, in_I, in_bm, out_vis;
   // workspace
   DevBuf freqs, beamT, ucoef, rec, counts, blkcounts, v, partial, tcgroups;
+  DevBuf umax, sortkv, crd_sorted, I_sorted;
 };
 
 namespace {
@@ -72,11 +78,27 @@ int fail(hv_context* c, int code, const char* fmt, ...) {
     ctx->launches += (n);      \
   } while (0)
 
+// A launch of a visibility-product kernel, bracketed by events when profiling.
+#define HV_LAUNCH_TIMED(call, st)                                   \
+  do {                                                              \
+    cudaEvent_t e0_ = nullptr, e1_ = nullptr;                       \
+    if (ctx->profiling) {                                           \
+      HV_CK(cudaEventCreate(&e0_));                                 \
+      HV_CK(cudaEventCreate(&e1_));                                 \
+      HV_CK(cudaEventRecord(e0_, (st)));                            \
+    }                                                               \
+    HV_LAUNCH(1, call);                                             \
+    if (ctx->profiling) {                                           \
+      HV_CK(cudaEventRecord(e1_, (st)));                            \
+      ctx->prof_events.emplace_back(e0_, e1_);                      \
+    }                                                               \
+  } while (0)
+
 int ensure(hv_context* ctx, DevBuf& b, size_t bytes) {
   if (bytes == 0) bytes = 256;
   if (b.cap >= bytes) return HV_OK;
-  // the old buffer may still be read by queued work
-  HV_CK(cudaStreamSynchronize(ctx->stream));
+  // the old buffer may still be read by queued work (on any stream)
+  HV_CK(cudaDeviceSynchronize());
   if (b.p) {
     HV_CK(cudaFree(b.p));
     ctx->held -= b.cap;
@@ -183,9 +205,28 @@ int run_device(hv_context* ctx, int method, const R* antpos, int nant, const dou
       HV_ENSURE(ctx->partial, sizeof(float) * slice_floats * (size_t)ntb * nfreq);
       HV_ENSURE(ctx->rec, sizeof(Rec) * (size_t)ntb * S1);
       HV_ENSURE(ctx->blkcounts, sizeof(int) * (size_t)prep_blocks(nsrc) * ntb);
+      // per-slice bound of |U|_1, and the catalogue in spatial order
+      HV_ENSURE(ctx->umax, sizeof(float) * (size_t)ntimes * nfreq);
+      HV_LAUNCH(1, launch_ubound(ctx->ucoef.p, ntimes * nfreq, Np,
+                                 static_cast<float*>(ctx->umax.p), st));
+      const R* crd_use = crd_eq;
+      const R* I_use = I_sky;
+      if (nsrc > 0) {
+        HV_ENSURE(ctx->sortkv, sizeof(unsigned long long) * (size_t)sort_pad(nsrc));
+        HV_ENSURE(ctx->crd_sorted, sizeof(float) * 3 * (size_t)nsrc);
+        HV_ENSURE(ctx->I_sorted, sizeof(float) * (size_t)nsrc);
+        int nl = 0;
+        HV_CK(launch_sort_sources(reinterpret_cast<const float*>(crd_eq),
+                                  reinterpret_cast<const float*>(I_sky), nsrc, ctx->sortkv.p,
+                                  static_cast<float*>(ctx->crd_sorted.p),
+                                  static_cast<float*>(ctx->I_sorted.p), &nl, st));
+        ctx->launches += nl;
+        crd_use = static_cast<const R*>(ctx->crd_sorted.p);
+        I_use = static_cast<const R*>(ctx->I_sorted.p);
+      }
       for (int t0 = 0; t0 < ntimes; t0 += ntb) {
         const int nt = std::min(ntb, ntimes - t0);
-        HV_LAUNCH(2, launch_prep<R>(crd_eq, I_sky, nsrc, eq2tops, t0, nt, P,
+        HV_LAUNCH(2, launch_prep<R>(crd_use, I_use, nsrc, eq2tops, t0, nt, P,
                                     static_cast<int*>(ctx->blkcounts.p), ctx->rec.p, counts + t0,
                                     st));
         TcLaunch L{};
@@ -196,6 +237,7 @@ int run_device(hv_context* ctx, int method, const R* antpos, int nant, const dou
         L.nf = nfreq;
         L.U = static_cast<const U*>(ctx->ucoef.p) + (size_t)t0 * nfreq * Np;
         L.beamT = reinterpret_cast<const float*>(beamT);
+        L.umax = static_cast<const float*>(ctx->umax.p) + (size_t)t0 * nfreq;
         L.Np = Np;
         L.nant = nant;
         L.P = P;
@@ -206,7 +248,7 @@ int run_device(hv_context* ctx, int method, const R* antpos, int nant, const dou
         L.max_slots = tc_max_slots(nant);
         L.err = ctx->d_err;
         L.num_sms = ctx->num_sms;
-        if (nsrc > 0) HV_LAUNCH(1, launch_tc(L, st));
+        if (nsrc > 0) HV_LAUNCH_TIMED(launch_tc(L, st), st);
         HV_LAUNCH(1, launch_reduce<float>(static_cast<float*>(ctx->partial.p), slice_floats,
                                           counts + t0, nt, nfreq, t0, ntimes, chunk, Np, nant,
                                           out, st));
@@ -229,8 +271,9 @@ int run_device(hv_context* ctx, int method, const R* antpos, int nant, const dou
       C* o = static_cast<C*>(out) + ((size_t)f * ntimes + t) * NN;
       HV_LAUNCH(1, launch_gen_phasors<R>(ctx->rec.p, counts + t, nsrc, Ut + (size_t)f * Np,
                                          beamT + (size_t)f * PP * Np, Np, nant, P, ctx->v.p, st));
-      HV_LAUNCH(1, launch_herk_plain<R>(ctx->v.p, counts + t, nsrc, Np,
-                                        static_cast<R*>(ctx->partial.p), st));
+      HV_LAUNCH_TIMED(launch_herk_plain<R>(ctx->v.p, counts + t, nsrc, Np,
+                                           static_cast<R*>(ctx->partial.p), st),
+                      st);
       HV_LAUNCH(1, launch_reduce<R>(static_cast<R*>(ctx->partial.p), 0, counts + t, 1, 1, 0, 1,
                                     kPlainChunk, Np, nant, o, st));
     }
@@ -256,6 +299,11 @@ int check_err_flag(hv_context* ctx) {
   HV_CK(cudaMemcpy(&flag, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (flag != 0) {
     HV_CK(cudaMemset(ctx->d_err, 0, sizeof(int)));
+    if (flag == 2)
+      return fail(ctx, HV_ERR_ARG,
+                  "antenna positions x frequency exceed the FP32 phase range of the tensor-core "
+                  "method (|U| >= 4e6 cycles); results of the last call are invalid, use the "
+                  "plain method");
     return fail(ctx, HV_ERR_TIMEOUT,
                 "a device-side wait gave up (code %d); results of the last call are invalid", flag);
   }
@@ -308,8 +356,13 @@ int hv_destroy(hv_context* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   DevBuf* bufs[] = {&ctx->in_antpos, &ctx->in_eq2tops, &ctx->in_crd, &ctx->in_I, &ctx->in_bm,
                     &ctx->out_vis, &ctx->freqs, &ctx->beamT, &ctx->ucoef, &ctx->rec,
-                    &ctx->counts, &ctx->blkcounts, &ctx->v, &ctx->partial, &ctx->tcgroups};
+                    &ctx->counts, &ctx->blkcounts, &ctx->v, &ctx->partial, &ctx->tcgroups,
+                    &ctx->umax, &ctx->sortkv, &ctx->crd_sorted, &ctx->I_sorted};
   for (DevBuf* b : bufs) release(ctx, *b);
+  for (auto& ev : ctx->prof_events) {
+    cudaEventDestroy(ev.first);
+    cudaEventDestroy(ev.second);
+  }
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -388,6 +441,32 @@ int hv_vis_gpu(hv_context* ctx, int precision, int method, const void* antpos, i
                const void* I_sky, int nsrc, const void* bm_cube, int beam_px, void* vis_out) {
   return hv_vis_multifreq(ctx, precision, method, antpos, nant, &freq, 1, eq2tops, ntimes,
                           crd_eq, I_sky, nsrc, bm_cube, beam_px, vis_out);
+}
+
+int hv_set_profiling(hv_context* ctx, int enable) {
+  if (!ctx) return HV_ERR_ARG;
+  ctx->profiling = enable != 0;
+  return HV_OK;
+}
+
+int hv_profile_read(hv_context* ctx, double* ms, uint64_t* launches) {
+  if (!ctx || !ms || !launches) return HV_ERR_ARG;
+  HV_CK(cudaSetDevice(ctx->device));
+  double total = 0.0;
+  for (auto& ev : ctx->prof_events) {
+    HV_CK(cudaEventSynchronize(ev.second));
+    float t = 0.f;
+    HV_CK(cudaEventElapsedTime(&t, ev.first, ev.second));
+    total += t;
+  }
+  *ms = total;
+  *launches = ctx->prof_events.size();
+  for (auto& ev : ctx->prof_events) {
+    cudaEventDestroy(ev.first);
+    cudaEventDestroy(ev.second);
+  }
+  ctx->prof_events.clear();
+  return HV_OK;
 }
 
 int hv_host_alloc(hv_context* ctx, size_t bytes, void** ptr) {

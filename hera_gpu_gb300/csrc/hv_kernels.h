@@ -32,6 +32,20 @@ cudaError_t launch_prep(const R* crd_eq, const R* I_sky, int nsrc, const R* eq2t
                         int t0, int nt, int P, int* block_counts, void* rec,
                         int* count, cudaStream_t st);
 
+// Bound max_a (|U_x| + |U_y| + |U_z|) of every (time, frequency) slice of U
+// (nslices x Np Ucoef32) into umax[nslices] (used by the fused kernel to
+// decide when a phase may be taken relative to a nearby source).
+cudaError_t launch_ubound(const void* U, int nslices, int Np, float* umax, cudaStream_t st);
+
+// --- hv_sort.cu ------------------------------------------------------------
+// Spatial (Morton) order of the sources: kv_buf needs sort_pad(nsrc) 64-bit
+// words; writes the permuted crd_eq (3 x nsrc) and I_sky.  *launches is set
+// to the number of kernels launched.
+int sort_pad(int nsrc);
+cudaError_t launch_sort_sources(const float* crd_eq, const float* I_sky, int nsrc, void* kv_buf,
+                                float* crd_sorted, float* I_sorted, int* launches,
+                                cudaStream_t st);
+
 // --- hv_plain.cu -----------------------------------------------------------
 // Source chunk of the split-K sum over sources (plain path).
 constexpr int kPlainChunk = 4096;
@@ -66,6 +80,7 @@ struct TcLaunch {
   const void* U;        // Ucoef32 [nt][nf][Np]
   const float* beamT;   // [nf][P*P][Np]
   int Np, nant, P;
+  const float* umax;    // [nt * nf] bound of |U|_1 per slice (launch_ubound)
   float* partial;       // [nt * nf][ceil(nsrc / chunk)][2][Np][Np]
   int chunk;            // sources per split-K chunk (multiple of 32)
   const void* groups;   // device copy of the group table (tc_fill_group_table)

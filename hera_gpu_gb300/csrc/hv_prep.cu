@@ -103,6 +103,29 @@ cudaError_t launch_ucoef(const R* antpos, int nant, int Np, const R* eq2tops, in
   return cudaGetLastError();
 }
 
+__global__ void __launch_bounds__(256)
+ubound_kernel(const Ucoef32* __restrict__ U, int Np, float* __restrict__ umax) {
+  __shared__ float red[8];
+  const Ucoef32* u = U + (size_t)blockIdx.x * Np;
+  float m = 0.f;
+  for (int a = threadIdx.x; a < Np; a += blockDim.x) {
+    const Ucoef32 c = u[a];
+    m = fmaxf(m, fabsf(c.hx) + fabsf(c.hy) + fabsf(c.hz));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < 8; ++w) m = fmaxf(m, red[w]);
+    umax[blockIdx.x] = m * 1.0001f;  // margin for the rounding of the sum
+  }
+}
+
+cudaError_t launch_ubound(const void* U, int nslices, int Np, float* umax, cudaStream_t st) {
+  ubound_kernel<<<nslices, 256, 0, st>>>(static_cast<const Ucoef32*>(U), Np, umax);
+  return cudaGetLastError();
+}
+
 // -------------------------------------------------------- source prep ----
 int prep_blocks(int nsrc) { return nsrc > 0 ? ceil_div(nsrc, kPrepBlock) : 1; }
 

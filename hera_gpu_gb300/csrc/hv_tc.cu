@@ -67,6 +67,7 @@ constexpr int TC_SMEM_LIMIT = 227 * 1024;
 constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // 2 s per wait
 
 constexpr int kErrTimeout = 1;
+constexpr int kErrRange = 2;    // |U| beyond the exact range of rint_magic
 
 struct TcGroup {
   int npairs, nslots;
@@ -83,6 +84,7 @@ struct TcParams {
   int nt, nf;           // times and frequencies of this launch
   const Ucoef32* U;     // [nt][nf][Np]
   const float* beamT;   // [nf][PP][Np]
+  const float* umax;    // [nt * nf] bound of |U|_1 per slice
   int Np, nant, PP, dx, dy;
   float* partial;       // [nt * nf][nchunk][2][Np][Np]
   int nchunk, chunk;
@@ -147,6 +149,7 @@ __device__ __forceinline__ bool wait_warp(uint32_t bar, uint32_t parity, volatil
   for (uint32_t i = 0;; ++i) {
     const bool done = mbar_try(bar, parity);
     if (__all_sync(0xffffffffu, done)) return true;
+    if (i >= 2) __nanosleep(64);  // leave issue slots to the MMA warp
     if ((i & 63) == 63) {
       int give_up = 0;
       if ((threadIdx.x & 31) == 0) {
@@ -195,15 +198,14 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms of
-// 1024 bytes (stride byte offset), sm_100 descriptor version 1.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
-  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)1 << 16;              // leading byte offset (unused for SW128 K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;    // stride byte offset
-  d |= (uint64_t)1 << 46;              // descriptor version
-  d |= (uint64_t)2 << 61;              // SWIZZLE_128B
-  return d;
+// Shared-memory matrix descriptor, K-major with the 128-byte swizzle: 8-row
+// atoms of 1024 bytes (stride byte offset), descriptor version 1 (sm_100
+// family).  The high word is the same for every operand; the low word holds
+// the start address (>> 4) and the leading byte offset (unused for this
+// layout).  Advancing along K by 32 bytes adds 2 to the low word.
+constexpr uint32_t kDescHi = (1024u >> 4) | (1u << 14) | (2u << 29);
+__device__ __forceinline__ uint32_t desc_lo(uint32_t saddr) {
+  return ((saddr & 0x3FFFFu) >> 4) | (1u << 16);
 }
 
 // Instruction descriptor, kind::f16: D F32, A and B BF16, both K-major,
@@ -216,13 +218,39 @@ __device__ __forceinline__ uint32_t idesc_bf16(int n, bool negate_a) {
   return d;
 }
 
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
-                                         uint32_t accumulate) {
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint32_t a_lo, uint32_t b_lo,
+                                         uint32_t idesc, uint32_t accumulate) {
   asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      "{\n .reg .pred p;\n .reg .b64 da, db;\n setp.ne.b32 p, %5, 0;\n"
+      " mov.b64 da, {%1, %3};\n mov.b64 db, {%2, %3};\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], da, db, %4, p;\n}\n" ::"r"(d_tmem),
+      "r"(a_lo), "r"(b_lo), "r"(kDescHi), "r"(idesc), "r"(accumulate)
       : "memory");
+}
+
+// The 24 MMAs of one block pair and one stage (32 sources): for each half
+// of the stage (16 sources) and each split product (hi hi, hi lo, lo hi),
+//   ReV += ReA ReB + ImA ImB,   ImV += ImA ReB - ReA ImB.
+// a, b: descriptor low words of the hi tiles of the pair's row and column
+// blocks (the lo tile follows 16 KB later).  first: the stage opens the item.
+__device__ __forceinline__ void issue_pair(uint32_t d_re, uint32_t a, uint32_t b, uint32_t idp,
+                                           uint32_t idn, bool first) {
+  const uint32_t d_im = d_re + 128;
+  const uint32_t A[2] = {a, a + (TC_HALF >> 4)};
+  const uint32_t B[2] = {b, b + (TC_HALF >> 4)};
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const uint32_t kre = 4u * h, kim = 4u * h + 2u;  // K-steps of 32 bytes
+#pragma unroll
+    for (int pr = 0; pr < 3; ++pr) {
+      const uint32_t aa = A[pr == 2 ? 1 : 0], bb = B[pr == 1 ? 1 : 0];
+      const uint32_t acc = (first && h == 0 && pr == 0) ? 0u : 1u;
+      mma_bf16(d_re, aa + kre, bb + kre, idp, acc);
+      mma_bf16(d_re, aa + kim, bb + kim, idp, 1u);
+      mma_bf16(d_im, aa + kim, bb + kre, idp, acc);
+      mma_bf16(d_im, aa + kre, bb + kim, idn, 1u);
+    }
+  }
 }
 
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
@@ -253,13 +281,45 @@ __device__ __forceinline__ void sts128(uint32_t addr, uint4 v) {
                : "memory");
 }
 
-__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
-  const uint32_t a = __bfloat16_as_ushort(__float2bfloat16_rn(lo));
-  const uint32_t b = __bfloat16_as_ushort(__float2bfloat16_rn(hi));
-  return a | (b << 16);
+// rint for |x| < 2^22 with two FP32 adds (FMA pipe) instead of FRND.
+__device__ __forceinline__ float rint_magic(float x) {
+  return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f);
 }
-__device__ __forceinline__ float bf16_round(float x) {
-  return __bfloat162float(__float2bfloat16_rn(x));
+
+// phase_cycles32 (hv_internal.cuh) with rint_magic: |U . s| < 2^21 cycles
+// is checked on the host before launch.
+__device__ __forceinline__ float phase_exact(const Ucoef32& u, float sx, float sy, float sz) {
+  const float p0 = __fmul_rn(u.hx, sx);
+  const float p1 = __fmul_rn(u.hy, sy);
+  const float p2 = __fmul_rn(u.hz, sz);
+  const float e0 = fmaf(u.hx, sx, -p0);
+  const float e1 = fmaf(u.hy, sy, -p1);
+  const float e2 = fmaf(u.hz, sz, -p2);
+  const float r0 = __fsub_rn(p0, rint_magic(p0));
+  const float r1 = __fsub_rn(p1, rint_magic(p1));
+  const float r2 = __fsub_rn(p2, rint_magic(p2));
+  const float lo = fmaf(u.lx, sx, fmaf(u.ly, sy, fmaf(u.lz, sz, __fadd_rn(__fadd_rn(e0, e1), e2))));
+  const float ph = __fadd_rn(__fadd_rn(r0, r1), __fadd_rn(r2, lo));
+  return __fsub_rn(ph, rint_magic(ph));
+}
+
+// Eight floats -> BF16 hi parts and BF16 residuals (v - hi), packed in
+// pairs (lower K index in the low half-word).
+__device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&h);
+}
+__device__ __forceinline__ void split_pack(const float* v, uint4& hi, uint4& lo) {
+  uint32_t h[4], l[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    h[i] = bf16x2_bits(v[2 * i], v[2 * i + 1]);
+    const float r0 = v[2 * i] - __uint_as_float(h[i] << 16);
+    const float r1 = v[2 * i + 1] - __uint_as_float(h[i] & 0xffff0000u);
+    l[i] = bf16x2_bits(r0, r1);
+  }
+  hi = make_uint4(h[0], h[1], h[2], h[3]);
+  lo = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
 // ------------------------------------------------------------- the kernel --
@@ -337,10 +397,18 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
     ItemInfo d;
     for (long long it = blockIdx.x; it < p.total_items; it += gridDim.x) {
       if (!decode_item(p, it, d)) continue;
-      const TcGroup grp = p.groups[d.g];
+      const TcGroup* gp = p.groups + d.g;
+      const int g_nslots = __ldg(&gp->nslots), g_npairs = __ldg(&gp->npairs);
+      const int g_rows0 = __ldg(&gp->slot_rows[0]), g_rows1 = __ldg(&gp->slot_rows[1]),
+                g_rows2 = __ldg(&gp->slot_rows[2]);
+      const int g_blk0 = __ldg(&gp->slot_block[0]), g_blk1 = __ldg(&gp->slot_block[1]),
+                g_blk2 = __ldg(&gp->slot_block[2]);
       const Ucoef32* Us = p.U + (size_t)d.sl * p.Np;
+      const float umax_sl = __ldg(p.umax + d.sl);
+      const float dlim = 8.0f / fmaxf(umax_sl, 1e-30f);
+      if (umax_sl >= 4.0e6f && tid == 0) atomicExch(p.err, kErrRange);
       const float* beam = p.beamT + (size_t)d.f * p.PP * p.Np;
-      const int nunits = grp.nslots * TC_ROWS * 4;
+      const int nunits = g_nslots * TC_ROWS * 4;
       bool ok = true;
       for (int j = 0; j < d.nst && ok; ++j, ++gs) {
         const int s = (int)(gs % NS);
@@ -352,8 +420,8 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
         const int src0 = d.s0 + j * TC_KS;
         for (int u = tid; u < nunits; u += TC_GEN_THREADS) {
           const int row = u & (TC_ROWS - 1);
-          const int slot = (u >> 7) % grp.nslots;
-          const int sg = (u >> 7) / grp.nslots;
+          const int slot = (u >> 7) % g_nslots;
+          const int sg = (u >> 7) / g_nslots;
           const int r8 = row & 7;
           const uint32_t rowoff = (uint32_t)(row >> 3) * 1024u + (uint32_t)r8 * 128u;
           const int h = sg >> 1, sub = sg & 1;
@@ -362,40 +430,62 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
           const uint32_t hi_tile = stage_op + (uint32_t)slot * TC_SLOT;
           const uint32_t lo_tile = hi_tile + TC_HALF;
           uint4 re_h = make_uint4(0, 0, 0, 0), im_h = re_h, re_l = re_h, im_l = re_h;
-          if (row < grp.slot_rows[slot]) {
-            const int a = grp.slot_block[slot] * TC_ROWS + row;
+          // per-slot fields selected without dynamic indexing (no local memory)
+          const int srows = slot == 0 ? g_rows0 : (slot == 1 ? g_rows1 : g_rows2);
+          const int sblk = slot == 0 ? g_blk0 : (slot == 1 ? g_blk1 : g_blk2);
+          if (row < srows) {
+            const int a = sblk * TC_ROWS + row;
             const Ucoef32 uc = Us[a];
             float rv[8], iv[8];
+            // the unit's first source is the phase reference: the other
+            // seven are, in spatial order, within dlim (|.|_1) of it, and
+            // U . (s - s_ref) < 8 cycles is accurate to ~1e-6 cycles in FP32
+            const float4* rp0 = reinterpret_cast<const float4*>(recs + sg * 8);
+            const float4 q0a = rp0[0];
+            const float ph_ref = phase_exact(uc, q0a.x, q0a.y, q0a.z);
+            int prev_pix = -1;
+            float b00 = 0.f, b01 = 0.f, b10 = 0.f, b11 = 0.f;
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-              const SrcRec32 r = recs[sg * 8 + q];
+              const float4* rp = reinterpret_cast<const float4*>(recs + sg * 8 + q);
+              const float4 ra = rp[0], rb = rp[1];  // sx sy sz amp | pix fx fy -
               float re = 0.f, im = 0.f;
               if (src0 + sg * 8 + q < d.s1) {
-                const float A = beam_bilinear<float>(beam, p.Np, a, r, p.dx, p.dy);
-                const float ph = phase_cycles32(uc, r.sx, r.sy, r.sz);
+                // warp-uniform: every lane (antenna) reads the same record
+                const int pix = __float_as_int(rb.x);
+                if (pix != prev_pix) {
+                  const float* bp = beam + (size_t)pix * p.Np + a;
+                  b00 = __ldg(bp);
+                  b01 = __ldg(bp + (size_t)p.dx * p.Np);
+                  b10 = __ldg(bp + (size_t)p.dy * p.Np);
+                  b11 = __ldg(bp + (size_t)(p.dx + p.dy) * p.Np);
+                  prev_pix = pix;
+                }
+                const float A = lerp(lerp(b00, b01, rb.y), lerp(b10, b11, rb.y), rb.z);
+                float ph;
+                const float dx = __fsub_rn(ra.x, q0a.x), dy = __fsub_rn(ra.y, q0a.y),
+                            dz = __fsub_rn(ra.z, q0a.z);
+                if (q == 0) {
+                  ph = ph_ref;
+                } else if (fabsf(dx) + fabsf(dy) + fabsf(dz) <= dlim) {
+                  ph = fmaf(uc.hx, dx, fmaf(uc.hy, dy, fmaf(uc.hz, dz, ph_ref)));
+                  ph = __fsub_rn(ph, rint_magic(ph));
+                } else {
+                  ph = phase_exact(uc, ra.x, ra.y, ra.z);
+                }
+                // the hardware sin/cos on [-pi, pi] (absolute error ~4e-7)
+                // is ample for BF16 operands
                 float sn, cs;
-                sincospif(2.0f * ph, &sn, &cs);
-                const float amp = A * r.amp;
+                __sincosf(6.28318530717958648f * ph, &sn, &cs);
+                const float amp = A * ra.w;
                 re = amp * cs;
                 im = amp * sn;
               }
               rv[q] = re;
               iv[q] = im;
             }
-            float rl[8], il[8];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-              rl[q] = rv[q] - bf16_round(rv[q]);
-              il[q] = iv[q] - bf16_round(iv[q]);
-            }
-            re_h = make_uint4(pack_bf16(rv[0], rv[1]), pack_bf16(rv[2], rv[3]),
-                              pack_bf16(rv[4], rv[5]), pack_bf16(rv[6], rv[7]));
-            im_h = make_uint4(pack_bf16(iv[0], iv[1]), pack_bf16(iv[2], iv[3]),
-                              pack_bf16(iv[4], iv[5]), pack_bf16(iv[6], iv[7]));
-            re_l = make_uint4(pack_bf16(rl[0], rl[1]), pack_bf16(rl[2], rl[3]),
-                              pack_bf16(rl[4], rl[5]), pack_bf16(rl[6], rl[7]));
-            im_l = make_uint4(pack_bf16(il[0], il[1]), pack_bf16(il[2], il[3]),
-                              pack_bf16(il[4], il[5]), pack_bf16(il[6], il[7]));
+            split_pack(rv, re_h, re_l);
+            split_pack(iv, im_h, im_l);
           }
           sts128(hi_tile + off_re, re_h);
           sts128(hi_tile + off_im, im_h);
@@ -412,8 +502,8 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
       {
         const int q = warp & 3, cb = warp >> 2;  // lane quadrant, 128-column block
         const int pr = cb >> 1, plane = cb & 1;
-        if (pr < grp.npairs) {
-          const int I = grp.pI[pr], J = grp.pJ[pr];
+        if (pr < g_npairs) {
+          const int I = __ldg(&gp->pI[pr]), J = __ldg(&gp->pJ[pr]);
           float* out = p.partial +
                        (((size_t)d.sl * p.nchunk + d.k) * 2 + plane) * (size_t)p.Np * p.Np;
           const int a = I * TC_ROWS + q * 32 + lane;
@@ -461,12 +551,15 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
       bool ok = true;
       for (long long it = blockIdx.x; it < p.total_items && ok; it += gridDim.x) {
         if (!decode_item(p, it, d)) continue;
-        const TcGroup grp = p.groups[d.g];
-        uint32_t idp[2], idn[2];
-        for (int q = 0; q < grp.npairs; ++q) {
-          idp[q] = idesc_bf16(grp.pN[q], false);
-          idn[q] = idesc_bf16(grp.pN[q], true);
-        }
+        const TcGroup* gp = p.groups + d.g;
+        const int n0 = __ldg(&gp->pN[0]), n1 = __ldg(&gp->pN[1]);
+        const uint32_t idp0 = idesc_bf16(n0, false), idn0 = idesc_bf16(n0, true);
+        const uint32_t idp1 = idesc_bf16(n1, false), idn1 = idesc_bf16(n1, true);
+        const uint32_t a0 = desc_lo(op_base + (uint32_t)__ldg(&gp->pa[0]) * TC_SLOT);
+        const uint32_t b0 = desc_lo(op_base + (uint32_t)__ldg(&gp->pb[0]) * TC_SLOT);
+        const uint32_t a1 = desc_lo(op_base + (uint32_t)__ldg(&gp->pa[1]) * TC_SLOT);
+        const uint32_t b1 = desc_lo(op_base + (uint32_t)__ldg(&gp->pb[1]) * TC_SLOT);
+        const bool two = __ldg(&gp->npairs) > 1;
         if (!wait1(acc_empty, (ic & 1) ^ 1, abort_flag, p.err)) { ok = false; break; }
         tc_fence_after();
         for (int j = 0; j < d.nst; ++j, ++gs) {
@@ -474,30 +567,9 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
           const uint32_t par = (gs / NS) & 1;
           if (!wait1(smem_full(s), par, abort_flag, p.err)) { ok = false; break; }
           tc_fence_after();
-          const uint32_t stage_op = op_base + (uint32_t)s * stage_bytes;
-          for (int q = 0; q < grp.npairs; ++q) {
-            const uint32_t a_hi = stage_op + (uint32_t)grp.pa[q] * TC_SLOT;
-            const uint32_t b_hi = stage_op + (uint32_t)grp.pb[q] * TC_SLOT;
-            const uint32_t A[2] = {a_hi, a_hi + TC_HALF};
-            const uint32_t B[2] = {b_hi, b_hi + TC_HALF};
-            const uint32_t d_re = tmem + (uint32_t)(q * 256);
-            const uint32_t d_im = d_re + 128;
-            // products (hi, hi), (hi, lo), (lo, hi)
-            const int pa_[3] = {0, 0, 1}, pb_[3] = {0, 1, 0};
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-              const uint32_t kre = (uint32_t)(2 * h) * 32u, kim = (uint32_t)(2 * h + 1) * 32u;
-#pragma unroll
-              for (int pr = 0; pr < 3; ++pr) {
-                const uint32_t first = (j == 0 && h == 0 && pr == 0) ? 0u : 1u;
-                const uint32_t a = A[pa_[pr]], b = B[pb_[pr]];
-                mma_bf16(d_re, sw128_desc(a + kre), sw128_desc(b + kre), idp[q], first);
-                mma_bf16(d_re, sw128_desc(a + kim), sw128_desc(b + kim), idp[q], 1u);
-                mma_bf16(d_im, sw128_desc(a + kim), sw128_desc(b + kre), idp[q], first);
-                mma_bf16(d_im, sw128_desc(a + kre), sw128_desc(b + kim), idn[q], 1u);
-              }
-            }
-          }
+          const uint32_t so = ((uint32_t)s * stage_bytes) >> 4;
+          issue_pair(tmem, a0 + so, b0 + so, idp0, idn0, j == 0);
+          if (two) issue_pair(tmem + 256, a1 + so, b1 + so, idp1, idn1, j == 0);
           mma_commit(smem_empty(s));
         }
         if (!ok) break;
@@ -633,6 +705,7 @@ cudaError_t launch_tc(const TcLaunch& L, cudaStream_t st) {
   p.nf = L.nf;
   p.U = static_cast<const Ucoef32*>(L.U);
   p.beamT = L.beamT;
+  p.umax = L.umax;
   p.Np = L.Np;
   p.nant = L.nant;
   p.PP = L.P * L.P;

@@ -99,11 +99,13 @@ def vis_gpu(antpos, freq, eq2tops, crd_eq, I_sky, bm_cube, real_dtype=None,
 
 
 def vis_gpu_multifreq(antpos, freqs, eq2tops, crd_eq, I_sky, bm_cubes, real_dtype=None,
-                      complex_dtype=None, precision=None, method="auto", context=None):
+                      complex_dtype=None, precision=None, method="auto", context=None, out=None):
     """Several frequencies in one call: ``bm_cubes`` (nfreq, nant, P, P) ->
     ``(nfreq, ntimes, nant, nant)``.  Equal to stacking ``vis_gpu`` per
     frequency (how the reference is driven for more than one channel), with
-    the source rotation and horizon cut shared across frequencies."""
+    the source rotation and horizon cut shared across frequencies.  ``out``
+    may supply the (nfreq, ntimes, nant, nant) result array (e.g. in
+    page-locked memory)."""
     antpos = np.asarray(antpos)
     eq2tops = np.asarray(eq2tops)
     crd_eq = np.asarray(crd_eq)
@@ -113,7 +115,10 @@ def vis_gpu_multifreq(antpos, freqs, eq2tops, crd_eq, I_sky, bm_cubes, real_dtyp
     prec, rt, ct = _resolve_precision(precision, real_dtype, complex_dtype)
     nant, npix, ntimes, beam_px = _check_shapes(antpos, eq2tops, crd_eq, I_sky, bm_cubes, True)
     assert bm_cubes.shape[0] == len(freqs)
-    out = np.empty((len(freqs), ntimes, nant, nant), dtype=ct)
+    if out is None:
+        out = np.empty((len(freqs), ntimes, nant, nant), dtype=ct)
+    assert out.shape == (len(freqs), ntimes, nant, nant) and out.dtype == ct
+    assert out.flags.c_contiguous
     ctx = context or _native.default_context()
     ctx.vis_multifreq(prec, method,
                       np.ascontiguousarray(antpos, dtype=rt), freqs,

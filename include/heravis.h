@@ -109,6 +109,14 @@ int hv_vis_multifreq_device(hv_context* ctx, int precision, int method,
  * (e.g. HV_ERR_TIMEOUT from a bounded wait). */
 int hv_sync(hv_context* ctx);
 
+/* Device timing of the visibility-product kernels (the fused tensor-core
+ * kernel, or the SIMT Hermitian product of the plain form): with profiling
+ * on, every launch of them is bracketed by CUDA events on the stream it runs
+ * on.  hv_profile_read() synchronises, returns the summed milliseconds and
+ * launch count since the previous read, and clears them. */
+int hv_set_profiling(hv_context* ctx, int enable);
+int hv_profile_read(hv_context* ctx, double* ms, uint64_t* launches);
+
 /* Page-locked host memory for fast host<->device copies (cudaHostAlloc). */
 int hv_host_alloc(hv_context* ctx, size_t bytes, void** ptr);
 int hv_host_free(hv_context* ctx, void* ptr);
