@@ -42,6 +42,8 @@ SIGNATURES = {
     "hv_sync": (_c_int, [_c_void_p]),
     "hv_set_profiling": (_c_int, [_c_void_p, _c_int]),
     "hv_profile_read": (_c_int, [_c_void_p, ctypes.POINTER(_c_double), ctypes.POINTER(ctypes.c_uint64)]),
+    "hv_vis_gpu_noalloc": (_c_int, [_PTR, _c_int, _c_double, _PTR, _c_int, _PTR, _PTR, _c_int,
+                                    _PTR, _c_int, _PTR, _c_void_p, ctypes.c_char_p, _c_size_t]),
     "hv_host_alloc": (_c_int, [_c_void_p, _c_size_t, ctypes.POINTER(_c_void_p)]),
     "hv_host_free": (_c_int, [_c_void_p, _c_void_p]),
 }

@@ -117,6 +117,26 @@ int hv_sync(hv_context* ctx);
 int hv_set_profiling(hv_context* ctx, int enable);
 int hv_profile_read(hv_context* ctx, double* ms, uint64_t* launches);
 
+/* No counterpart in the reference: an entry point for callers that cannot
+ * allocate device memory when they ask for visibilities (a real-time
+ * pipeline whose device memory is fixed before it starts, or a framework
+ * that owns the allocator).  Single frequency, precision 1, the plain form
+ * of the path (same kernels as hv_vis_multifreq_device with
+ * HV_METHOD_PLAIN); all inputs and the output (complex64 (ntimes, nant,
+ * nant)) are device pointers supplied by the caller, and the call allocates
+ * nothing: its working memory is one 64 MiB array per device, held from
+ * library load to process exit.  Requests needing more return HV_ERR_ARG
+ * with the byte count in `errbuf` (NUL-terminated, up to `errlen` bytes).
+ * The first call on a device looks the array up (make it before any stream
+ * capture); calls that overlap on the GPU share the array and race, so
+ * order them.  Asynchronous on `stream` (NULL = the legacy default stream);
+ * no context needed. */
+int hv_vis_gpu_noalloc(const void* d_antpos, int nant, double freq,
+                       const void* d_eq2tops, int ntimes,
+                       const void* d_crd_eq, const void* d_I_sky, int nsrc,
+                       const void* d_bm_cube, int beam_px, void* d_vis_out,
+                       void* stream, char* errbuf, size_t errlen);
+
 /* Page-locked host memory for fast host<->device copies (cudaHostAlloc). */
 int hv_host_alloc(hv_context* ctx, size_t bytes, void** ptr);
 int hv_host_free(hv_context* ctx, void* ptr);
