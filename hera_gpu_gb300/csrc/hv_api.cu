@@ -198,12 +198,13 @@ int run_device(hv_context* ctx, int method, const R* antpos, int nant, const dou
         chunk = tc_chunk_sources(S1, ntb * nfreq, ngroups, ctx->num_sms);
         slice_floats = tc_partial_floats(Np, S1, 1, chunk);
         const size_t pbytes = sizeof(float) * slice_floats * (size_t)ntb * nfreq;
-        const size_t rbytes = sizeof(Rec) * (size_t)ntb * S1;
+        const size_t rbytes = sizeof(Rec) * (size_t)ntb * (((size_t)S1 + 31) / 32 * 32);
         if (ntb == 1 || (pbytes <= kTcPartialCap && rbytes <= kTcRecCap)) break;
         ntb = (ntb + 1) / 2;
       }
       HV_ENSURE(ctx->partial, sizeof(float) * slice_floats * (size_t)ntb * nfreq);
-      HV_ENSURE(ctx->rec, sizeof(Rec) * (size_t)ntb * S1);
+      const size_t rec_stride = ((size_t)S1 + 31) / 32 * 32;  // whole stages per time
+      HV_ENSURE(ctx->rec, sizeof(Rec) * (size_t)ntb * rec_stride);
       HV_ENSURE(ctx->blkcounts, sizeof(int) * (size_t)prep_blocks(nsrc) * ntb);
       // per-slice bound of |U|_1, and the catalogue in spatial order
       HV_ENSURE(ctx->umax, sizeof(float) * (size_t)ntimes * nfreq);
@@ -226,11 +227,13 @@ int run_device(hv_context* ctx, int method, const R* antpos, int nant, const dou
       }
       for (int t0 = 0; t0 < ntimes; t0 += ntb) {
         const int nt = std::min(ntb, ntimes - t0);
-        HV_LAUNCH(2, launch_prep<R>(crd_use, I_use, nsrc, eq2tops, t0, nt, P,
-                                    static_cast<int*>(ctx->blkcounts.p), ctx->rec.p, counts + t0,
-                                    st));
+        HV_LAUNCH(2, launch_prep_strided<R>(crd_use, I_use, nsrc, eq2tops, t0, nt, P,
+                                            static_cast<int*>(ctx->blkcounts.p), ctx->rec.p,
+                                            rec_stride, counts + t0, st));
+        HV_LAUNCH(1, launch_tc_relative(ctx->rec.p, rec_stride, counts + t0, nt, nsrc, st));
         TcLaunch L{};
         L.rec = ctx->rec.p;
+        L.rec_stride = rec_stride;
         L.counts = counts + t0;
         L.nsrc = nsrc;
         L.nt = nt;

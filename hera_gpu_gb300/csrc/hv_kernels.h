@@ -46,6 +46,18 @@ cudaError_t launch_sort_sources(const float* crd_eq, const float* I_sky, int nsr
                                 float* crd_sorted, float* I_sorted, int* launches,
                                 cudaStream_t st);
 
+// launch_prep with records of time tt at rec + tt * rec_stride.
+template <typename R>
+cudaError_t launch_prep_strided(const R* crd_eq, const R* I_sky, int nsrc, const R* eq2tops,
+                                int t0, int nt, int P, int* block_counts, void* rec,
+                                size_t rec_stride, int* count, cudaStream_t st);
+
+// Fused-path record preparation (hv_prep.cu): per-unit spread of directions
+// in the pad word of each unit's first record, zero padding to a multiple of
+// 32 (rec_stride >= round_up(nsrc, 32)).
+cudaError_t launch_tc_relative(void* rec, size_t rec_stride, const int* counts, int nt, int nsrc,
+                               cudaStream_t st);
+
 // --- hv_plain.cu -----------------------------------------------------------
 // Source chunk of the split-K sum over sources (plain path).
 constexpr int kPlainChunk = 4096;
@@ -74,7 +86,8 @@ cudaError_t launch_reduce(const R* partial, size_t slice_stride, const int* coun
 
 // --- hv_tc.cu --------------------------------------------------------------
 struct TcLaunch {
-  const void* rec;      // SrcRec32 [nt][nsrc]
+  const void* rec;      // SrcRec32 [nt][rec_stride], rewritten by launch_tc_relative
+  size_t rec_stride;    // records per time, a multiple of 32 >= nsrc
   const int* counts;    // [nt]
   int nsrc, nt, nf;
   const void* U;        // Ucoef32 [nt][nf][Np]

@@ -14,6 +14,8 @@
 //    by every antenna and frequency.  Sources below the horizon are dropped
 //    (the reference computes them and multiplies by A = 0); the survivors keep
 //    their input order, so the split-K order is deterministic.
+#include <algorithm>
+
 #include "hv_internal.cuh"
 #include "hv_kernels.h"
 
@@ -190,7 +192,7 @@ __device__ __forceinline__ int beam_axis(double c, int P, double& w) {
 template <typename R>
 __global__ void __launch_bounds__(kPrepBlock)
 prep_write_kernel(const R* __restrict__ crd_eq, const R* __restrict__ I_sky, int nsrc,
-                  const R* __restrict__ eq2tops, int t0, int nblk, int P,
+                  size_t rec_stride, const R* __restrict__ eq2tops, int t0, int nblk, int P,
                   const int* __restrict__ block_counts,
                   typename Traits<R>::Rec* __restrict__ rec, int* __restrict__ count) {
   __shared__ double rot[9];
@@ -244,14 +246,14 @@ prep_write_kernel(const R* __restrict__ crd_eq, const R* __restrict__ I_sky, int
     const int py = beam_axis(ty, P, fy);
     typename Traits<R>::Rec r;
     fill_rec(r, x, y, z, sqrt((double)I_sky[s]), py * P + px, fx, fy);
-    rec[(size_t)tt * nsrc + idx] = r;
+    rec[(size_t)tt * rec_stride + idx] = r;
   }
 }
 
 template <typename R>
-cudaError_t launch_prep(const R* crd_eq, const R* I_sky, int nsrc, const R* eq2tops,
-                        int t0, int nt, int P, int* block_counts, void* rec,
-                        int* count, cudaStream_t st) {
+cudaError_t launch_prep_strided(const R* crd_eq, const R* I_sky, int nsrc, const R* eq2tops,
+                                int t0, int nt, int P, int* block_counts, void* rec,
+                                size_t rec_stride, int* count, cudaStream_t st) {
   const int nblk = prep_blocks(nsrc);
   dim3 grid(nblk, nt);
   prep_count_kernel<R><<<grid, kPrepBlock, 0, st>>>(crd_eq, nsrc, eq2tops, t0, nblk,
@@ -259,8 +261,61 @@ cudaError_t launch_prep(const R* crd_eq, const R* I_sky, int nsrc, const R* eq2t
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   prep_write_kernel<R><<<grid, kPrepBlock, 0, st>>>(
-      crd_eq, I_sky, nsrc, eq2tops, t0, nblk, P, block_counts,
+      crd_eq, I_sky, nsrc, rec_stride, eq2tops, t0, nblk, P, block_counts,
       reinterpret_cast<typename Traits<R>::Rec*>(rec), count);
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_prep(const R* crd_eq, const R* I_sky, int nsrc, const R* eq2tops,
+                        int t0, int nt, int P, int* block_counts, void* rec,
+                        int* count, cudaStream_t st) {
+  return launch_prep_strided<R>(crd_eq, I_sky, nsrc, eq2tops, t0, nt, P, block_counts, rec,
+                                (size_t)nsrc, count, st);
+}
+
+// ---------------------------------------------------- fused-path records --
+// Prepares the records of each time for the fused kernel, in place:
+//  * record 0 of each unit of 8 consecutive records (the 8 sources one
+//    generator thread handles together) gets, in its pad word, the largest
+//    |s - s_ref|_1 over the unit (s_ref = record 0's direction): the fused
+//    kernel takes phases relative to s_ref when that is small enough for the
+//    slice at hand;
+//  * records [count, round_up(count, 32)) are zeroed, so a partial last stage
+//    reads sources of zero amplitude at beam pixel 0.
+__global__ void __launch_bounds__(256)
+tc_relative_kernel(SrcRec32* __restrict__ rec, size_t rec_stride,
+                   const int* __restrict__ counts) {
+  const int tt = blockIdx.y;
+  SrcRec32* r = rec + (size_t)tt * rec_stride;
+  const int n = counts[tt];
+  const int npad = (n + 31) & ~31;
+  for (int i0 = blockIdx.x * blockDim.x; i0 < npad; i0 += gridDim.x * blockDim.x) {
+    const int i = i0 + threadIdx.x;  // a warp covers 4 whole units
+    float d1 = 0.f;
+    float ref_x = 0.f, ref_y = 0.f, ref_z = 0.f;
+    if (i < n) {
+      const SrcRec32 ref = r[i & ~7];
+      const SrcRec32 me = r[i];
+      ref_x = ref.sx; ref_y = ref.sy; ref_z = ref.sz;
+      d1 = fabsf(me.sx - ref_x) + fabsf(me.sy - ref_y) + fabsf(me.sz - ref_z);
+    }
+    // max over the 8 lanes of the unit
+    for (int o = 4; o > 0; o >>= 1) d1 = fmaxf(d1, __shfl_xor_sync(0xffffffffu, d1, o));
+    __syncwarp();
+    if (i < n) {
+      if ((i & 7) == 0) r[i].pad = __float_as_int(d1);
+    } else if (i < npad) {
+      r[i] = SrcRec32{};
+    }
+  }
+}
+
+cudaError_t launch_tc_relative(void* rec, size_t rec_stride, const int* counts, int nt, int nsrc,
+                               cudaStream_t st) {
+  const int blocks = std::max(1, std::min(ceil_div(nsrc, 256), 2048));
+  dim3 grid(blocks, nt);
+  tc_relative_kernel<<<grid, 256, 0, st>>>(static_cast<SrcRec32*>(rec), rec_stride, counts);
   return cudaGetLastError();
 }
 
@@ -269,6 +324,7 @@ template cudaError_t launch_beam_transpose<double>(const double*, int, int, int,
 template cudaError_t launch_ucoef<float>(const float*, int, int, const float*, int, int, const double*, int, void*, cudaStream_t);
 template cudaError_t launch_ucoef<double>(const double*, int, int, const double*, int, int, const double*, int, void*, cudaStream_t);
 template cudaError_t launch_prep<float>(const float*, const float*, int, const float*, int, int, int, int*, void*, int*, cudaStream_t);
+template cudaError_t launch_prep_strided<float>(const float*, const float*, int, const float*, int, int, int, int*, void*, size_t, int*, cudaStream_t);
 template cudaError_t launch_prep<double>(const double*, const double*, int, const double*, int, int, int, int*, void*, int*, cudaStream_t);
 
 }  // namespace hv

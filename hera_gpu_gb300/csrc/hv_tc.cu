@@ -80,7 +80,8 @@ struct TcGroup {
 
 struct TcParams {
   const int* counts;    // [nt] sources above the horizon per time
-  int nsrc;             // records per time in the record tensor
+  int nsrc;             // catalogue size (bounds the split-K chunks)
+  int rec_stride;       // records per time in the record tensor
   int nt, nf;           // times and frequencies of this launch
   const Ucoef32* U;     // [nt][nf][Np]
   const float* beamT;   // [nf][PP][Np]
@@ -322,6 +323,61 @@ __device__ __forceinline__ void split_pack(const float* v, uint4& hi, uint4& lo)
   lo = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
+// Phasors of 8 consecutive records (one unit) for one antenna: v = A sqrt(I)
+// e^{2 pi i phi}.  Record 0's direction is the unit's reference; its pad word
+// holds the largest |s - s_ref|_1 of the unit (tc_relative_kernel).  When
+// that is below dlim = 8 / max_a |U_a|_1 for this slice, the phases are
+// U . s_ref (exact) + U . (s - s_ref), the second term below 8 cycles and so
+// rounded to ~1e-6 cycles in FP32; otherwise every phase is computed exactly.
+// All lanes read the same records, so the branch does not diverge.  Padding
+// records have zero amplitude.  beam_a: the antenna's column of the
+// transposed beam.
+template <bool kNear>
+__device__ __forceinline__ void gen_unit_path(const SrcRec32* rec, const Ucoef32& uc,
+                                              const float* beam_a, int Np, int dx, int dy,
+                                              float4 ref, float ph_ref, float* rv, float* iv) {
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const float4* rp = reinterpret_cast<const float4*>(rec + q);
+    const float4 ra = rp[0], rb = rp[1];  // sx sy sz amp | pix fx fy -
+    const float* bp = beam_a + (size_t)__float_as_int(rb.x) * Np;
+    const float b00 = __ldg(bp), b01 = __ldg(bp + (size_t)dx * Np);
+    const float b10 = __ldg(bp + (size_t)dy * Np), b11 = __ldg(bp + (size_t)(dx + dy) * Np);
+    const float A = lerp(lerp(b00, b01, rb.y), lerp(b10, b11, rb.y), rb.z);
+    float ph;
+    if (!kNear) {
+      ph = phase_exact(uc, ra.x, ra.y, ra.z);
+    } else if (q == 0) {
+      ph = ph_ref;
+    } else {
+      const float ex = __fsub_rn(ra.x, ref.x), ey = __fsub_rn(ra.y, ref.y),
+                  ez = __fsub_rn(ra.z, ref.z);
+      ph = fmaf(uc.hx, ex, fmaf(uc.hy, ey, fmaf(uc.hz, ez, ph_ref)));
+      ph = __fsub_rn(ph, rint_magic(ph));
+    }
+    // the hardware sin/cos on [-pi, pi] (absolute error ~4e-7) is ample for
+    // BF16 operands
+    float sn, cs;
+    __sincosf(6.28318530717958648f * ph, &sn, &cs);
+    const float amp = A * ra.w;
+    rv[q] = amp * cs;
+    iv[q] = amp * sn;
+  }
+}
+
+__device__ __forceinline__ void gen_unit(const SrcRec32* rec, const Ucoef32& uc,
+                                         const float* beam_a, int Np, int dx, int dy, float dlim,
+                                         float* rv, float* iv) {
+  const float4* rp0 = reinterpret_cast<const float4*>(rec);
+  const float4 q0a = rp0[0], q0b = rp0[1];
+  if (__int_as_float(__float_as_int(q0b.w)) <= dlim) {
+    const float ph_ref = phase_exact(uc, q0a.x, q0a.y, q0a.z);
+    gen_unit_path<true>(rec, uc, beam_a, Np, dx, dy, q0a, ph_ref, rv, iv);
+  } else {
+    gen_unit_path<false>(rec, uc, beam_a, Np, dx, dy, q0a, 0.f, rv, iv);
+  }
+}
+
 // ------------------------------------------------------------- the kernel --
 struct ItemInfo {
   int g, k, tl, f, sl;
@@ -405,10 +461,27 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
                 g_blk2 = __ldg(&gp->slot_block[2]);
       const Ucoef32* Us = p.U + (size_t)d.sl * p.Np;
       const float umax_sl = __ldg(p.umax + d.sl);
-      const float dlim = 8.0f / fmaxf(umax_sl, 1e-30f);
       if (umax_sl >= 4.0e6f && tid == 0) atomicExch(p.err, kErrRange);
+      const float dlim = 8.0f / fmaxf(umax_sl, 1e-30f);
       const float* beam = p.beamT + (size_t)d.f * p.PP * p.Np;
-      const int nunits = g_nslots * TC_ROWS * 4;
+      // this thread's units (fixed for the item): u = tid + i * 512
+      int u_slot[3], u_sg[3], u_a[3];
+      bool u_ok[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const int u = tid + i * TC_GEN_THREADS;
+        const int slot = (u >> 7) % g_nslots;
+        u_slot[i] = slot;
+        u_sg[i] = (u >> 7) / g_nslots;
+        const int row = u & (TC_ROWS - 1);
+        const int srows = slot == 0 ? g_rows0 : (slot == 1 ? g_rows1 : g_rows2);
+        const int sblk = slot == 0 ? g_blk0 : (slot == 1 ? g_blk1 : g_blk2);
+        u_ok[i] = i < g_nslots && row < srows;
+        u_a[i] = sblk * TC_ROWS + row;
+      }
+      const int row = tid & (TC_ROWS - 1);
+      const int r8 = row & 7;
+      const uint32_t rowoff = (uint32_t)(row >> 3) * 1024u + (uint32_t)r8 * 128u;
       bool ok = true;
       for (int j = 0; j < d.nst && ok; ++j, ++gs) {
         const int s = (int)(gs % NS);
@@ -417,73 +490,19 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
         if (!wait_warp(smem_empty(s), par ^ 1, abort_flag, p.err)) { ok = false; break; }
         const SrcRec32* recs = reinterpret_cast<const SrcRec32*>(rec_smem + (size_t)s * TC_REC);
         const uint32_t stage_op = op_base + (uint32_t)s * stage_bytes;
-        const int src0 = d.s0 + j * TC_KS;
-        for (int u = tid; u < nunits; u += TC_GEN_THREADS) {
-          const int row = u & (TC_ROWS - 1);
-          const int slot = (u >> 7) % g_nslots;
-          const int sg = (u >> 7) / g_nslots;
-          const int r8 = row & 7;
-          const uint32_t rowoff = (uint32_t)(row >> 3) * 1024u + (uint32_t)r8 * 128u;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          if (i >= g_nslots) continue;
+          const int sg = u_sg[i];
           const int h = sg >> 1, sub = sg & 1;
           const uint32_t off_re = rowoff + ((uint32_t)((4 * h + sub) ^ r8) << 4);
           const uint32_t off_im = rowoff + ((uint32_t)((4 * h + 2 + sub) ^ r8) << 4);
-          const uint32_t hi_tile = stage_op + (uint32_t)slot * TC_SLOT;
+          const uint32_t hi_tile = stage_op + (uint32_t)u_slot[i] * TC_SLOT;
           const uint32_t lo_tile = hi_tile + TC_HALF;
           uint4 re_h = make_uint4(0, 0, 0, 0), im_h = re_h, re_l = re_h, im_l = re_h;
-          // per-slot fields selected without dynamic indexing (no local memory)
-          const int srows = slot == 0 ? g_rows0 : (slot == 1 ? g_rows1 : g_rows2);
-          const int sblk = slot == 0 ? g_blk0 : (slot == 1 ? g_blk1 : g_blk2);
-          if (row < srows) {
-            const int a = sblk * TC_ROWS + row;
-            const Ucoef32 uc = Us[a];
+          if (u_ok[i]) {
             float rv[8], iv[8];
-            // the unit's first source is the phase reference: the other
-            // seven are, in spatial order, within dlim (|.|_1) of it, and
-            // U . (s - s_ref) < 8 cycles is accurate to ~1e-6 cycles in FP32
-            const float4* rp0 = reinterpret_cast<const float4*>(recs + sg * 8);
-            const float4 q0a = rp0[0];
-            const float ph_ref = phase_exact(uc, q0a.x, q0a.y, q0a.z);
-            int prev_pix = -1;
-            float b00 = 0.f, b01 = 0.f, b10 = 0.f, b11 = 0.f;
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-              const float4* rp = reinterpret_cast<const float4*>(recs + sg * 8 + q);
-              const float4 ra = rp[0], rb = rp[1];  // sx sy sz amp | pix fx fy -
-              float re = 0.f, im = 0.f;
-              if (src0 + sg * 8 + q < d.s1) {
-                // warp-uniform: every lane (antenna) reads the same record
-                const int pix = __float_as_int(rb.x);
-                if (pix != prev_pix) {
-                  const float* bp = beam + (size_t)pix * p.Np + a;
-                  b00 = __ldg(bp);
-                  b01 = __ldg(bp + (size_t)p.dx * p.Np);
-                  b10 = __ldg(bp + (size_t)p.dy * p.Np);
-                  b11 = __ldg(bp + (size_t)(p.dx + p.dy) * p.Np);
-                  prev_pix = pix;
-                }
-                const float A = lerp(lerp(b00, b01, rb.y), lerp(b10, b11, rb.y), rb.z);
-                float ph;
-                const float dx = __fsub_rn(ra.x, q0a.x), dy = __fsub_rn(ra.y, q0a.y),
-                            dz = __fsub_rn(ra.z, q0a.z);
-                if (q == 0) {
-                  ph = ph_ref;
-                } else if (fabsf(dx) + fabsf(dy) + fabsf(dz) <= dlim) {
-                  ph = fmaf(uc.hx, dx, fmaf(uc.hy, dy, fmaf(uc.hz, dz, ph_ref)));
-                  ph = __fsub_rn(ph, rint_magic(ph));
-                } else {
-                  ph = phase_exact(uc, ra.x, ra.y, ra.z);
-                }
-                // the hardware sin/cos on [-pi, pi] (absolute error ~4e-7)
-                // is ample for BF16 operands
-                float sn, cs;
-                __sincosf(6.28318530717958648f * ph, &sn, &cs);
-                const float amp = A * ra.w;
-                re = amp * cs;
-                im = amp * sn;
-              }
-              rv[q] = re;
-              iv[q] = im;
-            }
+            gen_unit(recs + sg * 8, Us[u_a[i]], beam + u_a[i], p.Np, p.dx, p.dy, dlim, rv, iv);
             split_pack(rv, re_h, re_l);
             split_pack(iv, im_h, im_l);
           }
@@ -536,7 +555,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
           if (!wait1(smem_full(s), par ^ 1, abort_flag, p.err)) { ok = false; break; }
           mbar_expect_tx(rec_full(s), TC_REC);
           tma_load_2d(rec_base + (uint32_t)s * TC_REC, &rec_map, rec_full(s), 0,
-                      d.tl * p.nsrc + d.s0 + j * TC_KS);
+                      d.tl * p.rec_stride + d.s0 + j * TC_KS);
         }
       }
       // let the copies still in flight land before the CTA can exit
@@ -688,7 +707,7 @@ cudaError_t launch_tc(const TcLaunch& L, cudaStream_t st) {
   auto encode = encode_fn();
   if (!encode) return cudaErrorNotSupported;
   CUtensorMap map;
-  const cuuint64_t gdim[2] = {8, (cuuint64_t)L.nt * L.nsrc};
+  const cuuint64_t gdim[2] = {8, (cuuint64_t)L.nt * L.rec_stride};
   const cuuint64_t gstride[1] = {sizeof(SrcRec32)};
   const cuuint32_t box[2] = {8, TC_KS};
   const cuuint32_t estride[2] = {1, 1};
@@ -701,6 +720,7 @@ cudaError_t launch_tc(const TcLaunch& L, cudaStream_t st) {
   TcParams p{};
   p.counts = L.counts;
   p.nsrc = L.nsrc;
+  p.rec_stride = (int)L.rec_stride;
   p.nt = L.nt;
   p.nf = L.nf;
   p.U = static_cast<const Ucoef32*>(L.U);
