@@ -61,13 +61,16 @@ constexpr int TC_GEN_WARPS = 16;
 constexpr int TC_GEN_THREADS = TC_GEN_WARPS * 32;
 constexpr int TC_PRODUCER_WARP = TC_GEN_WARPS;
 constexpr int TC_MMA_WARP = TC_GEN_WARPS + 1;
-constexpr int TC_THREADS = TC_GEN_THREADS + 64;
+constexpr int TC_PUSH_WARP = TC_GEN_WARPS + 2;  // cluster mode: pushes tiles to peer CTAs
+constexpr int TC_THREADS = TC_GEN_THREADS + 96;
 constexpr int TC_TMEM_COLS = 512;
 constexpr int TC_SMEM_LIMIT = 227 * 1024;
 constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // 2 s per wait
 
 constexpr int kErrTimeout = 1;
 constexpr int kErrRange = 2;    // |U| beyond the exact range of rint_magic
+
+constexpr int TC_MAX_CLUSTER = 8;
 
 struct TcGroup {
   int npairs, nslots;
@@ -76,6 +79,19 @@ struct TcGroup {
   int pa[2], pb[2];  // slots of the row (A) and column (B) operands of each pair
   int pI[2], pJ[2];  // block indices of each pair
   int pN[2];         // MMA N of each pair (valid columns of block J, multiple of 16)
+  // Cluster mode (one CTA per group, cluster rank = group index): every
+  // block is generated by exactly one CTA of the cluster and written into
+  // the shared memory of each CTA whose group uses it.
+  int nown;                            // slots generated here
+  int own_slot[3];                     // ... which ones
+  int ndst[3];                         // per owned slot: other CTAs it goes to
+  int dst_rank[3][TC_MAX_CLUSTER - 1];
+  int dst_slot[3][TC_MAX_CLUSTER - 1];
+  int recv_slots;                      // slots pushed here by peers per stage
+  int full_count;                      // arrivals per stage on this CTA's smem_full
+  int empty_count;                     // arrivals per stage on this CTA's smem_empty
+  int commit_mask;                     // CTAs this CTA's MMA completion is signalled to
+  int write_mask;                      // CTAs this CTA's generators write to (bit = rank)
 };
 
 struct TcParams {
@@ -126,12 +142,16 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Single-thread bounded wait.
+__device__ __forceinline__ bool mbar_try_cluster(uint32_t bar, uint32_t parity);
+
+// Single-thread bounded wait (kCl: acquire at cluster scope, for barriers
+// that threads of other CTAs arrive on).
+template <bool kCl = false>
 __device__ __forceinline__ bool wait1(uint32_t bar, uint32_t parity, volatile int* abort_flag,
                                       int* gerr) {
   const unsigned long long t0 = global_ns();
   for (uint32_t i = 0;; ++i) {
-    if (mbar_try(bar, parity)) return true;
+    if (kCl ? mbar_try_cluster(bar, parity) : mbar_try(bar, parity)) return true;
     if ((i & 63) == 63) {
       if (*abort_flag) return false;
       if (global_ns() - t0 > TC_WAIT_NS) {
@@ -144,11 +164,12 @@ __device__ __forceinline__ bool wait1(uint32_t bar, uint32_t parity, volatile in
 }
 
 // Whole-warp bounded wait; the outcome is uniform across the warp.
+template <bool kCl = false>
 __device__ __forceinline__ bool wait_warp(uint32_t bar, uint32_t parity, volatile int* abort_flag,
                                           int* gerr) {
   const unsigned long long t0 = global_ns();
   for (uint32_t i = 0;; ++i) {
-    const bool done = mbar_try(bar, parity);
+    const bool done = kCl ? mbar_try_cluster(bar, parity) : mbar_try(bar, parity);
     if (__all_sync(0xffffffffu, done)) return true;
     if (i >= 2) __nanosleep(64);  // leave issue slots to the MMA warp
     if ((i & 63) == 63) {
@@ -178,6 +199,65 @@ __device__ __forceinline__ void wait_drain(uint32_t bar, uint32_t parity, int* g
       return;
     }
   }
+}
+
+// cluster-scope variants (distributed shared memory)
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t map_to_rank(uint32_t saddr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void sts128_cluster(uint32_t addr, uint4 v) {
+  asm volatile("st.shared::cluster.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x),
+               "r"(v.y), "r"(v.z), "r"(v.w)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t remote_bar) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(remote_bar)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_cluster(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void fence_async_smem_cluster() {
+  asm volatile("fence.proxy.async.shared::cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mma_commit_multicast(uint32_t bar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64"
+      " [%0], %1;" ::"r"(bar), "h"(mask)
+      : "memory");
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::
+                   : "memory");
+}
+
+// Copy engine push of `bytes` from this CTA's shared memory to a peer's
+// (dst and its barrier given as cluster addresses); completion is signalled
+// on the peer's barrier as transaction bytes.
+__device__ __forceinline__ void bulk_push(uint32_t dst_cluster, uint32_t src_cta, uint32_t bytes,
+                                          uint32_t bar_cluster) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      ::"r"(dst_cluster), "r"(src_cta), "r"(bytes), "r"(bar_cluster)
+      : "memory");
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_all() {
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
 __device__ __forceinline__ void fence_async_smem() {
@@ -384,9 +464,19 @@ struct ItemInfo {
   int s0, s1, nst;
 };
 
-__device__ __forceinline__ bool decode_item(const TcParams& p, long long it, ItemInfo& d) {
-  d.g = (int)(it % p.ngroups);
-  const long long rest = it / p.ngroups;
+// Item it -> (group, chunk, slice).  Without clusters an item is one group of
+// one (slice, chunk); in cluster mode an item is a (slice, chunk) and every
+// CTA of the cluster takes its own group (its rank).
+template <bool kCluster>
+__device__ __forceinline__ bool decode_item(const TcParams& p, long long it, int rank,
+                                            ItemInfo& d) {
+  long long rest = it;
+  if (kCluster) {
+    d.g = rank;
+  } else {
+    d.g = (int)(it % p.ngroups);
+    rest = it / p.ngroups;
+  }
   d.k = (int)(rest % p.nchunk);
   d.sl = (int)(rest / p.nchunk);
   d.tl = d.sl / p.nf;
@@ -399,6 +489,9 @@ __device__ __forceinline__ bool decode_item(const TcParams& p, long long it, Ite
   return true;
 }
 
+// 18 warps on 4 schedulers: the busiest scheduler holds 5 warps, and its
+// 16K-register file caps a thread at 96 registers (launch bounds give that).
+template <bool kCluster>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
   extern __shared__ uint8_t smem_raw[];
@@ -415,24 +508,39 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
   auto rec_full = [&](int s) { return bar0 + 8u * s; };
   auto smem_full = [&](int s) { return bar0 + 8u * (NS + s); };
   auto smem_empty = [&](int s) { return bar0 + 8u * (2 * NS + s); };
-  const uint32_t acc_full = bar0 + 8u * (3 * NS);
+  auto rec_empty = [&](int s) { return bar0 + 8u * (3 * NS + s); };
+  auto gen_done = [&](int s) { return bar0 + 8u * (4 * NS + s); };
+  const uint32_t acc_full = bar0 + 8u * (5 * NS);
   const uint32_t acc_empty = acc_full + 8;
   const uint32_t drain = acc_full + 16;
-  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 3 * NS + 3);
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 5 * NS + 3);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int rank = kCluster ? (int)cluster_rank() : 0;
+  const long long it0 = kCluster ? blockIdx.x / p.ngroups : blockIdx.x;
+  const long long istep = kCluster ? gridDim.x / p.ngroups : gridDim.x;
+  const TcGroup* mine = p.groups + rank;  // cluster mode: this CTA's group
+  // cluster mode: operand bytes this CTA receives from peers per stage
+  const uint32_t recv_bytes = kCluster ? (uint32_t)__ldg(&mine->recv_slots) * TC_SLOT : 0u;
   if (threadIdx.x == 0) {
+    const int full_count = kCluster ? mine->full_count : TC_GEN_WARPS;
+    const int empty_count = kCluster ? mine->empty_count : 1;
     for (int s = 0; s < NS; ++s) {
       mbar_init(rec_full(s), 1);
-      mbar_init(smem_full(s), TC_GEN_THREADS);
-      mbar_init(smem_empty(s), 1);
+      mbar_init(smem_full(s), full_count);
+      mbar_init(smem_empty(s), empty_count);
+      mbar_init(rec_empty(s), TC_GEN_WARPS);
+      mbar_init(gen_done(s), TC_GEN_WARPS);
     }
     mbar_init(acc_full, 1);
     mbar_init(acc_empty, TC_GEN_THREADS);
     mbar_init(drain, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    // the first round of every stage expects the peers' pushed tiles
+    if (recv_bytes)
+      for (int s = 0; s < NS; ++s) mbar_expect_tx(smem_full(s), recv_bytes);
   }
   if (warp == TC_MMA_WARP) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -443,16 +551,21 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
   }
   tc_fence_before();
   __syncthreads();
+  // peers may arrive on our barriers only once every CTA has initialised them
+  if (kCluster) cluster_sync_all();
   tc_fence_after();
   const uint32_t tmem = *tmem_holder;
+  // cluster mode: does this CTA generate any block?
+  const int nown = kCluster ? __ldg(&mine->nown) : 0;
+  const bool generates = !kCluster || nown > 0;
 
   if (warp < TC_GEN_WARPS) {
     // ------------------------------------------------ phasor generators --
     const int tid = threadIdx.x;
     uint32_t gs = 0, ic = 0;
     ItemInfo d;
-    for (long long it = blockIdx.x; it < p.total_items; it += gridDim.x) {
-      if (!decode_item(p, it, d)) continue;
+    for (long long it = it0; it < p.total_items; it += istep) {
+      if (!decode_item<kCluster>(p, it, rank, d)) continue;
       const TcGroup* gp = p.groups + d.g;
       const int g_nslots = __ldg(&gp->nslots), g_npairs = __ldg(&gp->npairs);
       const int g_rows0 = __ldg(&gp->slot_rows[0]), g_rows1 = __ldg(&gp->slot_rows[1]),
@@ -464,35 +577,38 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
       if (umax_sl >= 4.0e6f && tid == 0) atomicExch(p.err, kErrRange);
       const float dlim = 8.0f / fmaxf(umax_sl, 1e-30f);
       const float* beam = p.beamT + (size_t)d.f * p.PP * p.Np;
+      // the slots this CTA fills: all of its group's (no clusters) or the
+      // ones it owns (cluster mode)
+      const int nfill = kCluster ? nown : g_nslots;
       // this thread's units (fixed for the item): u = tid + i * 512
       int u_slot[3], u_sg[3], u_a[3];
       bool u_ok[3];
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
         const int u = tid + i * TC_GEN_THREADS;
-        const int slot = (u >> 7) % g_nslots;
+        const int k = (u >> 7) % max(nfill, 1);
+        const int slot = kCluster ? __ldg(&gp->own_slot[min(k, 2)]) : k;
         u_slot[i] = slot;
-        u_sg[i] = (u >> 7) / g_nslots;
+        u_sg[i] = (u >> 7) / max(nfill, 1);
         const int row = u & (TC_ROWS - 1);
         const int srows = slot == 0 ? g_rows0 : (slot == 1 ? g_rows1 : g_rows2);
         const int sblk = slot == 0 ? g_blk0 : (slot == 1 ? g_blk1 : g_blk2);
-        u_ok[i] = i < g_nslots && row < srows;
+        u_ok[i] = i < nfill && row < srows;
         u_a[i] = sblk * TC_ROWS + row;
       }
       const int row = tid & (TC_ROWS - 1);
       const int r8 = row & 7;
       const uint32_t rowoff = (uint32_t)(row >> 3) * 1024u + (uint32_t)r8 * 128u;
+      const int wmask = kCluster ? __ldg(&gp->write_mask) : 1;
       bool ok = true;
-      for (int j = 0; j < d.nst && ok; ++j, ++gs) {
+      for (int j = 0; j < d.nst && ok && generates; ++j, ++gs) {
         const int s = (int)(gs % NS);
         const uint32_t par = (gs / NS) & 1;
         if (!wait_warp(rec_full(s), par, abort_flag, p.err)) { ok = false; break; }
-        if (!wait_warp(smem_empty(s), par ^ 1, abort_flag, p.err)) { ok = false; break; }
+        if (!wait_warp<kCluster>(smem_empty(s), par ^ 1, abort_flag, p.err)) { ok = false; break; }
         const SrcRec32* recs = reinterpret_cast<const SrcRec32*>(rec_smem + (size_t)s * TC_REC);
         const uint32_t stage_op = op_base + (uint32_t)s * stage_bytes;
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          if (i >= g_nslots) continue;
+        auto unit = [&](int i) {
           const int sg = u_sg[i];
           const int h = sg >> 1, sub = sg & 1;
           const uint32_t off_re = rowoff + ((uint32_t)((4 * h + sub) ^ r8) << 4);
@@ -510,9 +626,24 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
           sts128(hi_tile + off_im, im_h);
           sts128(lo_tile + off_re, re_l);
           sts128(lo_tile + off_im, im_l);
+        };
+        if (kCluster) {
+#pragma unroll 1
+          for (int i = 0; i < nfill; ++i) unit(i);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+            if (i < nfill) unit(i);
         }
+        // operands of this stage written: one arrival per warp (each lane
+        // fences its own writes for the tensor core and the copy engine)
         fence_async_smem();
-        mbar_arrive(smem_full(s));
+        __syncwarp();
+        if (lane == 0) {
+          mbar_arrive(smem_full(s));
+          if (kCluster) mbar_arrive(gen_done(s));
+          mbar_arrive(rec_empty(s));  // the records may be reloaded
+        }
       }
       if (!ok) break;
       // ------------------------------------------------------- epilogue --
@@ -542,17 +673,17 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
     }
   } else if (warp == TC_PRODUCER_WARP) {
     // ----------------------------------------------------- TMA producer --
-    if (lane == 0) {
+    if (lane == 0 && generates) {
       uint32_t gs = 0;
       ItemInfo d;
       bool ok = true;
-      for (long long it = blockIdx.x; it < p.total_items && ok; it += gridDim.x) {
-        if (!decode_item(p, it, d)) continue;
+      for (long long it = it0; it < p.total_items && ok; it += istep) {
+        if (!decode_item<kCluster>(p, it, rank, d)) continue;
         for (int j = 0; j < d.nst; ++j, ++gs) {
           const int s = (int)(gs % NS);
           const uint32_t par = (gs / NS) & 1;
-          // the generators have finished with the previous round of this slot
-          if (!wait1(smem_full(s), par ^ 1, abort_flag, p.err)) { ok = false; break; }
+          // this CTA's generators have finished reading the previous round
+          if (!wait1(rec_empty(s), par ^ 1, abort_flag, p.err)) { ok = false; break; }
           mbar_expect_tx(rec_full(s), TC_REC);
           tma_load_2d(rec_base + (uint32_t)s * TC_REC, &rec_map, rec_full(s), 0,
                       d.tl * p.rec_stride + d.s0 + j * TC_KS);
@@ -562,14 +693,15 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
       const uint32_t first = gs > (uint32_t)NS ? gs - NS : 0;
       for (uint32_t g = first; g < gs; ++g) wait_drain(rec_full((int)(g % NS)), (g / NS) & 1, p.err);
     }
-  } else {
+  } else if (warp == TC_MMA_WARP) {
     // ------------------------------------------------------- MMA issuer --
     if (lane == 0) {
       uint32_t gs = 0, ic = 0;
       ItemInfo d;
       bool ok = true;
-      for (long long it = blockIdx.x; it < p.total_items && ok; it += gridDim.x) {
-        if (!decode_item(p, it, d)) continue;
+      const uint16_t cmask = kCluster ? (uint16_t)__ldg(&mine->commit_mask) : (uint16_t)1;
+      for (long long it = it0; it < p.total_items && ok; it += istep) {
+        if (!decode_item<kCluster>(p, it, rank, d)) continue;
         const TcGroup* gp = p.groups + d.g;
         const int n0 = __ldg(&gp->pN[0]), n1 = __ldg(&gp->pN[1]);
         const uint32_t idp0 = idesc_bf16(n0, false), idn0 = idesc_bf16(n0, true);
@@ -585,11 +717,17 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
           const int s = (int)(gs % NS);
           const uint32_t par = (gs / NS) & 1;
           if (!wait1(smem_full(s), par, abort_flag, p.err)) { ok = false; break; }
+          // arm the next round of this stage for the peers' pushes (they can
+          // only come after this round's MMAs release the slot)
+          if (recv_bytes) mbar_expect_tx(smem_full(s), recv_bytes);
           tc_fence_after();
           const uint32_t so = ((uint32_t)s * stage_bytes) >> 4;
           issue_pair(tmem, a0 + so, b0 + so, idp0, idn0, j == 0);
           if (two) issue_pair(tmem + 256, a1 + so, b1 + so, idp1, idn1, j == 0);
-          mma_commit(smem_empty(s));
+          // the stage's slots may be refilled -- here and, in cluster mode,
+          // by the CTAs that wrote them -- once these MMAs have read them
+          if (kCluster && cmask != (uint16_t)(1u << rank)) mma_commit_multicast(smem_empty(s), cmask);
+          else mma_commit(smem_empty(s));
         }
         if (!ok) break;
         mma_commit(acc_full);
@@ -601,8 +739,36 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
     }
   }
 
+  if (kCluster && warp == TC_PUSH_WARP && lane == 0 && nown > 0) {
+    // ---------------------------------------------- DSMEM tile pusher --
+    uint32_t gs = 0;
+    ItemInfo d;
+    bool ok = true;
+    for (long long it = it0; it < p.total_items && ok; it += istep) {
+      if (!decode_item<kCluster>(p, it, rank, d)) continue;
+      for (int j = 0; j < d.nst; ++j, ++gs) {
+        const int s = (int)(gs % NS);
+        const uint32_t par = (gs / NS) & 1;
+        if (!wait1(gen_done(s), par, abort_flag, p.err)) { ok = false; break; }
+        const uint32_t stage_op = op_base + (uint32_t)s * stage_bytes;
+        for (int k = 0; k < nown; ++k) {
+          const uint32_t src = stage_op + (uint32_t)__ldg(&mine->own_slot[k]) * TC_SLOT;
+          const int nd = __ldg(&mine->ndst[k]);
+          for (int q = 0; q < nd; ++q) {
+            const uint32_t rr = (uint32_t)__ldg(&mine->dst_rank[k][q]);
+            const uint32_t dst = stage_op + (uint32_t)__ldg(&mine->dst_slot[k][q]) * TC_SLOT;
+            bulk_push(map_to_rank(dst, rr), src, TC_SLOT, map_to_rank(smem_full(s), rr));
+          }
+        }
+      }
+    }
+    bulk_wait_all();
+  }
+
   tc_fence_before();
   __syncthreads();
+  // no CTA leaves while a peer may still write to its shared memory
+  if (kCluster) cluster_sync_all();
   if (warp == TC_MMA_WARP) {
     __syncwarp();
     tc_fence_after();
@@ -669,6 +835,68 @@ std::vector<TcGroup> make_groups(int nant) {
   return out;
 }
 
+// Cluster mode: each block is generated by one CTA of the cluster (among
+// the groups that use it, the one with the fewest generated rows so far) and
+// sent to the others; fills the sharing fields of every group.
+void plan_cluster(std::vector<TcGroup>& gs, int nant) {
+  const int C = (int)gs.size();
+  const int nb = ceil_div(nant, TC_ROWS);
+  std::vector<int> load(C, 0);
+  auto slot_in = [&](int g, int blk) {
+    for (int s = 0; s < gs[g].nslots; ++s)
+      if (gs[g].slot_block[s] == blk) return s;
+    return -1;
+  };
+  for (auto& g : gs) {
+    g.nown = 0;
+    g.write_mask = 0;
+  }
+  for (int b = 0; b < nb; ++b) {
+    int owner = -1;
+    for (int g = 0; g < C; ++g)
+      if (slot_in(g, b) >= 0 && (owner < 0 || load[g] < load[owner])) owner = g;
+    if (owner < 0) continue;
+    load[owner] += std::min(TC_ROWS, nant - b * TC_ROWS);
+    TcGroup& o = gs[owner];
+    const int k = o.nown++;
+    o.own_slot[k] = slot_in(owner, b);
+    o.ndst[k] = 0;
+    o.write_mask |= 1 << owner;
+    for (int g = 0; g < C; ++g) {
+      if (g == owner || slot_in(g, b) < 0) continue;
+      o.dst_rank[k][o.ndst[k]] = g;
+      o.dst_slot[k][o.ndst[k]] = slot_in(g, b);
+      ++o.ndst[k];
+      o.write_mask |= 1 << g;
+    }
+  }
+  for (int x = 0; x < C; ++x) {
+    int writers = 0, commit = 1 << x, targets = 0;
+    for (int o = 0; o < C; ++o) {
+      if ((gs[o].write_mask >> x) & 1) {
+        ++writers;
+        commit |= 1 << o;
+      }
+      if (o != x && ((gs[x].write_mask >> o) & 1)) ++targets;
+    }
+    // local generator warps (if this CTA generates) + the MMA thread's arming
+    // of the bytes pushed by peers
+    int recv = 0;
+    for (int o = 0; o < C; ++o)
+      if (o != x)
+        for (int k = 0; k < gs[o].nown; ++k)
+          for (int q = 0; q < gs[o].ndst[k]; ++q)
+            if (gs[o].dst_rank[k][q] == x) ++recv;
+    gs[x].recv_slots = recv;
+    gs[x].full_count = (gs[x].nown > 0 ? TC_GEN_WARPS : 0) + (recv > 0 ? 1 : 0);
+    (void)writers;
+    gs[x].commit_mask = commit;
+    gs[x].empty_count = 1 + targets;
+  }
+}
+
+bool use_cluster(int ngroups) { return ngroups > 1 && ngroups <= TC_MAX_CLUSTER; }
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   if (!fn) {
@@ -689,7 +917,8 @@ int tc_num_groups(int nant) { return (int)make_groups(nant).size(); }
 size_t tc_group_table_bytes(int nant) { return sizeof(TcGroup) * make_groups(nant).size(); }
 
 int tc_fill_group_table(int nant, void* host_buf) {
-  const auto g = make_groups(nant);
+  auto g = make_groups(nant);
+  if (use_cluster((int)g.size())) plan_cluster(g, nant);
   std::copy(g.begin(), g.end(), static_cast<TcGroup*>(host_buf));
   return (int)g.size();
 }
@@ -744,11 +973,38 @@ cudaError_t launch_tc(const TcLaunch& L, cudaStream_t st) {
   p.nstages = std::min(4, (TC_SMEM_LIMIT - fixed) / per_stage);
   if (p.nstages < 2) return cudaErrorInvalidConfiguration;
   const int smem = fixed + p.nstages * per_stage;
-  cudaError_t e = cudaFuncSetAttribute(tc_vis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e = cudaFuncSetAttribute(tc_vis_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        smem);
   if (e != cudaSuccess) return e;
-  const long long grid = std::min<long long>(L.num_sms, p.total_items);
-  tc_vis_kernel<<<(int)grid, TC_THREADS, smem, st>>>(map, p);
+  if (!use_cluster(p.ngroups)) {
+    const long long grid = std::min<long long>(L.num_sms, p.total_items);
+    tc_vis_kernel<false><<<(int)grid, TC_THREADS, smem, st>>>(map, p);
+    return cudaGetLastError();
+  }
+  // cluster mode: one CTA per group, items are (slice, chunk)
+  p.total_items = (long long)L.nt * L.nf * p.nchunk;
+  e = cudaFuncSetAttribute(tc_vis_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)p.ngroups;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(TC_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cfg.gridDim = dim3((unsigned)(p.ngroups * (L.num_sms / p.ngroups)));
+  int nclusters = 0;
+  e = cudaOccupancyMaxActiveClusters(&nclusters, tc_vis_kernel<true>, &cfg);
+  if (e != cudaSuccess) return e;
+  if (nclusters < 1) return cudaErrorInvalidConfiguration;
+  nclusters = (int)std::min<long long>(nclusters, p.total_items);
+  cfg.gridDim = dim3((unsigned)(p.ngroups * nclusters));
+  e = cudaLaunchKernelEx(&cfg, tc_vis_kernel<true>, map, p);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 
