@@ -278,9 +278,10 @@ cudaError_t launch_prep(const R* crd_eq, const R* I_sky, int nsrc, const R* eq2t
 // Prepares the records of each time for the fused kernel, in place:
 //  * record 0 of each unit of 8 consecutive records (the 8 sources one
 //    generator thread handles together) gets, in its pad word, the largest
-//    |s - s_ref|_1 over the unit (s_ref = record 0's direction): the fused
-//    kernel takes phases relative to s_ref when that is small enough for the
-//    slice at hand;
+//    |s - s_ref|_1 over the unit (s_ref = record 0's direction), with the
+//    sign bit set if all eight share record 0's beam pixel: the fused kernel
+//    takes phases relative to s_ref when the spread is small enough for the
+//    slice at hand, and loads the four beam corners once for such a unit;
 //  * records [count, round_up(count, 32)) are zeroed, so a partial last stage
 //    reads sources of zero amplitude at beam pixel 0.
 __global__ void __launch_bounds__(256)
@@ -293,18 +294,24 @@ tc_relative_kernel(SrcRec32* __restrict__ rec, size_t rec_stride,
   for (int i0 = blockIdx.x * blockDim.x; i0 < npad; i0 += gridDim.x * blockDim.x) {
     const int i = i0 + threadIdx.x;  // a warp covers 4 whole units
     float d1 = 0.f;
-    float ref_x = 0.f, ref_y = 0.f, ref_z = 0.f;
+    int pix = -1, ref_pix = -1;
     if (i < n) {
       const SrcRec32 ref = r[i & ~7];
       const SrcRec32 me = r[i];
-      ref_x = ref.sx; ref_y = ref.sy; ref_z = ref.sz;
-      d1 = fabsf(me.sx - ref_x) + fabsf(me.sy - ref_y) + fabsf(me.sz - ref_z);
+      d1 = fabsf(me.sx - ref.sx) + fabsf(me.sy - ref.sy) + fabsf(me.sz - ref.sz);
+      pix = me.pix;
+      ref_pix = ref.pix;
     }
-    // max over the 8 lanes of the unit
+    // over the 8 lanes of the unit: largest spread, and whether every
+    // source sits on the reference's beam pixel (padding counts as same)
     for (int o = 4; o > 0; o >>= 1) d1 = fmaxf(d1, __shfl_xor_sync(0xffffffffu, d1, o));
+    const unsigned differ = __ballot_sync(0xffffffffu, i < n && pix != ref_pix);
+    const bool same_pix = ((differ >> (threadIdx.x & 24)) & 0xffu) == 0;
     __syncwarp();
     if (i < n) {
-      if ((i & 7) == 0) r[i].pad = __float_as_int(d1);
+      // pad word of the unit's first record: the spread as a float, with the
+      // sign bit set when all eight sources share one beam pixel
+      if ((i & 7) == 0) r[i].pad = __float_as_int(d1) | (same_pix ? (int)0x80000000u : 0);
     } else if (i < npad) {
       r[i] = SrcRec32{};
     }

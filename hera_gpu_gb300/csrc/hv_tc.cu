@@ -405,24 +405,39 @@ __device__ __forceinline__ void split_pack(const float* v, uint4& hi, uint4& lo)
 
 // Phasors of 8 consecutive records (one unit) for one antenna: v = A sqrt(I)
 // e^{2 pi i phi}.  Record 0's direction is the unit's reference; its pad word
-// holds the largest |s - s_ref|_1 of the unit (tc_relative_kernel).  When
+// holds the largest |s - s_ref|_1 of the unit (tc_relative_kernel), its sign
+// bit set when all eight sources share a beam pixel (then the four corners
+// are loaded once for the unit).  When
 // that is below dlim = 8 / max_a |U_a|_1 for this slice, the phases are
 // U . s_ref (exact) + U . (s - s_ref), the second term below 8 cycles and so
 // rounded to ~1e-6 cycles in FP32; otherwise every phase is computed exactly.
 // All lanes read the same records, so the branch does not diverge.  Padding
 // records have zero amplitude.  beam_a: the antenna's column of the
 // transposed beam.
-template <bool kNear>
+template <bool kNear, bool kOnePixel>
 __device__ __forceinline__ void gen_unit_path(const SrcRec32* rec, const Ucoef32& uc,
                                               const float* beam_a, int Np, int dx, int dy,
                                               float4 ref, float ph_ref, float* rv, float* iv) {
+  float c00 = 0.f, c01 = 0.f, c10 = 0.f, c11 = 0.f;
+  if (kOnePixel) {
+    const float* bp = beam_a + (size_t)__float_as_int(reinterpret_cast<const float4*>(rec)[1].x) * Np;
+    c00 = __ldg(bp);
+    c01 = __ldg(bp + (size_t)dx * Np);
+    c10 = __ldg(bp + (size_t)dy * Np);
+    c11 = __ldg(bp + (size_t)(dx + dy) * Np);
+  }
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
     const float4* rp = reinterpret_cast<const float4*>(rec + q);
     const float4 ra = rp[0], rb = rp[1];  // sx sy sz amp | pix fx fy -
-    const float* bp = beam_a + (size_t)__float_as_int(rb.x) * Np;
-    const float b00 = __ldg(bp), b01 = __ldg(bp + (size_t)dx * Np);
-    const float b10 = __ldg(bp + (size_t)dy * Np), b11 = __ldg(bp + (size_t)(dx + dy) * Np);
+    float b00 = c00, b01 = c01, b10 = c10, b11 = c11;
+    if (!kOnePixel) {
+      const float* bp = beam_a + (size_t)__float_as_int(rb.x) * Np;
+      b00 = __ldg(bp);
+      b01 = __ldg(bp + (size_t)dx * Np);
+      b10 = __ldg(bp + (size_t)dy * Np);
+      b11 = __ldg(bp + (size_t)(dx + dy) * Np);
+    }
     const float A = lerp(lerp(b00, b01, rb.y), lerp(b10, b11, rb.y), rb.z);
     float ph;
     if (!kNear) {
@@ -450,11 +465,15 @@ __device__ __forceinline__ void gen_unit(const SrcRec32* rec, const Ucoef32& uc,
                                          float* rv, float* iv) {
   const float4* rp0 = reinterpret_cast<const float4*>(rec);
   const float4 q0a = rp0[0], q0b = rp0[1];
-  if (__int_as_float(__float_as_int(q0b.w)) <= dlim) {
+  const int flags = __float_as_int(q0b.w);
+  const bool one_pixel = flags < 0;
+  const bool near = __int_as_float(flags & 0x7fffffff) <= dlim;
+  if (near) {
     const float ph_ref = phase_exact(uc, q0a.x, q0a.y, q0a.z);
-    gen_unit_path<true>(rec, uc, beam_a, Np, dx, dy, q0a, ph_ref, rv, iv);
+    if (one_pixel) gen_unit_path<true, true>(rec, uc, beam_a, Np, dx, dy, q0a, ph_ref, rv, iv);
+    else gen_unit_path<true, false>(rec, uc, beam_a, Np, dx, dy, q0a, ph_ref, rv, iv);
   } else {
-    gen_unit_path<false>(rec, uc, beam_a, Np, dx, dy, q0a, 0.f, rv, iv);
+    gen_unit_path<false, false>(rec, uc, beam_a, Np, dx, dy, q0a, 0.f, rv, iv);
   }
 }
 
