@@ -23,6 +23,19 @@ HV_ERR_UNSUPPORTED = 5
 
 METHODS = {"auto": 0, "plain": 1, "tc": 2, "tc_bf16": 2}
 
+class HvSim(ctypes.Structure):
+    """hv_sim of include/heravis.h: one simulation of a batch (device
+    pointers, except freqs which is a host pointer)."""
+    _fields_ = [("antpos", ctypes.c_void_p), ("eq2tops", ctypes.c_void_p),
+                ("crd_eq", ctypes.c_void_p), ("I_sky", ctypes.c_void_p),
+                ("bm_cubes", ctypes.c_void_p), ("freqs", ctypes.c_void_p),
+                ("vis_out", ctypes.c_void_p), ("nant", ctypes.c_int), ("ntimes", ctypes.c_int),
+                ("nsrc", ctypes.c_int), ("nfreq", ctypes.c_int), ("beam_px", ctypes.c_int)]
+
+
+HV_BATCH_GRAPH = 1
+HV_BATCH_AUTOTUNE = 2
+
 # Every function of the ABI: name -> (restype, argtypes)
 _c_int, _c_void_p, _c_size_t, _c_double = ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_double
 _PTR = ctypes.c_void_p
@@ -44,6 +57,13 @@ SIGNATURES = {
     "hv_profile_read": (_c_int, [_c_void_p, ctypes.POINTER(_c_double), ctypes.POINTER(ctypes.c_uint64)]),
     "hv_vis_gpu_noalloc": (_c_int, [_PTR, _c_int, _c_double, _PTR, _c_int, _PTR, _PTR, _c_int,
                                     _PTR, _c_int, _PTR, _c_void_p, ctypes.c_char_p, _c_size_t]),
+    "hv_batch_create": (_c_int, [_c_void_p, ctypes.POINTER(HvSim), _c_int, ctypes.c_uint,
+                                 ctypes.POINTER(_c_void_p)]),
+    "hv_batch_launch": (_c_int, [_c_void_p, _c_void_p]),
+    "hv_batch_sync": (_c_int, [_c_void_p]),
+    "hv_batch_launches": (ctypes.c_uint64, [_c_void_p]),
+    "hv_batch_destroy": (_c_int, [_c_void_p]),
+    "hv_vis_batch": (_c_int, [_c_void_p, ctypes.POINTER(HvSim), _c_int, _c_void_p]),
     "hv_host_alloc": (_c_int, [_c_void_p, _c_size_t, ctypes.POINTER(_c_void_p)]),
     "hv_host_free": (_c_int, [_c_void_p, _c_void_p]),
 }
@@ -179,6 +199,47 @@ class Context:
         buf = (ctypes.c_byte * nbytes).from_address(p.value)
         weakref.finalize(buf, self.lib.hv_host_free, self.h, ctypes.c_void_p(p.value))
         return np.frombuffer(buf, dtype=dtype, count=n).reshape(shape)
+
+
+class Batch:
+    """A planned batch of simulations (hv_batch_create).  ``sims`` is a list
+    of dicts of device pointers / sizes (see HvSim); ``freqs`` of each is a
+    numpy float64 array kept alive here."""
+
+    def __init__(self, ctx: "Context", sims, graph=False, autotune=False):
+        self.ctx = ctx
+        self._freqs = [np.ascontiguousarray(s["freqs"], dtype=np.float64) for s in sims]
+        arr = (HvSim * len(sims))()
+        for i, s in enumerate(sims):
+            arr[i] = HvSim(s["antpos"], s["eq2tops"], s["crd_eq"], s["I_sky"], s["bm_cubes"],
+                           self._freqs[i].ctypes.data, s["vis_out"], s["nant"], s["ntimes"],
+                           s["nsrc"], len(self._freqs[i]), s["beam_px"])
+        self._arr = arr
+        h = ctypes.c_void_p()
+        flags = (HV_BATCH_GRAPH if graph else 0) | (HV_BATCH_AUTOTUNE if autotune else 0)
+        ctx.check(ctx.lib.hv_batch_create(ctx.h, arr, len(sims), flags, ctypes.byref(h)))
+        self.h = h
+
+    @property
+    def launches(self) -> int:
+        return int(self.ctx.lib.hv_batch_launches(self.h))
+
+    def launch(self, stream=0):
+        self.ctx.check(self.ctx.lib.hv_batch_launch(self.h, ctypes.c_void_p(stream)))
+
+    def sync(self):
+        self.ctx.check(self.ctx.lib.hv_batch_sync(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.hv_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 _contexts = {}

@@ -30,6 +30,10 @@ struct DevBuf {
   void* p = nullptr;
   size_t cap = 0;
 };
+struct HostBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+};
 
 }  // namespace
 
@@ -50,7 +54,8 @@ struct hv_context {
   DevBuf in_antpos, in_eq2tops, in_crd, in_I, in_bm, out_vis;
   // workspace
   DevBuf freqs, beamT, ucoef, rec, counts, blkcounts, v, partial, tcgroups;
-  DevBuf umax, sortkv, crd_sorted, I_sorted;
+  DevBuf umax, sortkv, crd_sorted, I_sorted, tctable;
+  HostBuf tctable_h;  // page-locked staging of the fused kernel's simulation table
 };
 
 namespace {
@@ -120,6 +125,24 @@ int ensure(hv_context* ctx, DevBuf& b, size_t bytes) {
   ctx->held += want;
   return HV_OK;
 }
+
+// Page-locked host buffer that stays valid for the copies queued from it.
+int ensure_host(hv_context* ctx, HostBuf& b, size_t bytes) {
+  if (b.cap >= bytes) return HV_OK;
+  HV_CK(cudaDeviceSynchronize());
+  if (b.p) HV_CK(cudaFreeHost(b.p));
+  b.p = nullptr;
+  b.cap = 0;
+  HV_CK(cudaHostAlloc(&b.p, bytes, cudaHostAllocDefault));
+  b.cap = bytes;
+  return HV_OK;
+}
+
+#define HV_HOST_ENSURE(buf, bytes)               \
+  do {                                           \
+    int r_ = ensure_host(ctx, (buf), (bytes));   \
+    if (r_ != HV_OK) return r_;                  \
+  } while (0)
 
 #define HV_ENSURE(buf, bytes)                 \
   do {                                        \
@@ -231,27 +254,31 @@ int run_device(hv_context* ctx, int method, const R* antpos, int nant, const dou
                                             static_cast<int*>(ctx->blkcounts.p), ctx->rec.p,
                                             rec_stride, counts + t0, st));
         HV_LAUNCH(1, launch_tc_relative(ctx->rec.p, rec_stride, counts + t0, nt, nsrc, st));
-        TcLaunch L{};
-        L.rec = ctx->rec.p;
-        L.rec_stride = rec_stride;
+        TcSimDesc L{};
         L.counts = counts + t0;
-        L.nsrc = nsrc;
-        L.nt = nt;
-        L.nf = nfreq;
         L.U = static_cast<const U*>(ctx->ucoef.p) + (size_t)t0 * nfreq * Np;
         L.beamT = reinterpret_cast<const float*>(beamT);
         L.umax = static_cast<const float*>(ctx->umax.p) + (size_t)t0 * nfreq;
-        L.Np = Np;
-        L.nant = nant;
-        L.P = P;
         L.partial = static_cast<float*>(ctx->partial.p);
-        L.chunk = chunk;
         L.groups = ctx->tcgroups.p;
         L.ngroups = ngroups;
         L.max_slots = tc_max_slots(nant);
-        L.err = ctx->d_err;
-        L.num_sms = ctx->num_sms;
-        if (nsrc > 0) HV_LAUNCH_TIMED(launch_tc(L, st), st);
+        L.rec_row0 = 0;
+        L.rec_stride = (int)rec_stride;
+        L.nt = nt;
+        L.nf = nfreq;
+        L.Np = Np;
+        L.nant = nant;
+        L.P = P;
+        L.nsrc = nsrc;
+        L.chunk = chunk;
+        HV_ENSURE(ctx->tctable, tc_sim_table_bytes(1));
+        HV_HOST_ENSURE(ctx->tctable_h, tc_sim_table_bytes(1));
+        if (nsrc > 0)
+          HV_LAUNCH_TIMED(launch_tc_batch(&L, 1, ctx->rec.p, (long long)nt * rec_stride,
+                                          ctx->tctable.p, ctx->tctable_h.p, ctx->d_err,
+                                          ctx->num_sms, st),
+                          st);
         HV_LAUNCH(1, launch_reduce<float>(static_cast<float*>(ctx->partial.p), slice_floats,
                                           counts + t0, nt, nfreq, t0, ntimes, chunk, Np, nant,
                                           out, st));
@@ -315,6 +342,10 @@ int check_err_flag(hv_context* ctx) {
 
 }  // namespace
 
+cudaStream_t hv_context_stream(hv_context* ctx) { return ctx->stream; }
+void hv_context_set_error(hv_context* ctx, const char* msg) { ctx->err = msg; }
+void hv_context_add_launches(hv_context* ctx, uint64_t n) { ctx->launches += n; }
+
 extern "C" {
 
 int hv_version(void) { return 10000; }
@@ -360,8 +391,9 @@ int hv_destroy(hv_context* ctx) {
   DevBuf* bufs[] = {&ctx->in_antpos, &ctx->in_eq2tops, &ctx->in_crd, &ctx->in_I, &ctx->in_bm,
                     &ctx->out_vis, &ctx->freqs, &ctx->beamT, &ctx->ucoef, &ctx->rec,
                     &ctx->counts, &ctx->blkcounts, &ctx->v, &ctx->partial, &ctx->tcgroups,
-                    &ctx->umax, &ctx->sortkv, &ctx->crd_sorted, &ctx->I_sorted};
+                    &ctx->umax, &ctx->sortkv, &ctx->crd_sorted, &ctx->I_sorted, &ctx->tctable};
   for (DevBuf* b : bufs) release(ctx, *b);
+  if (ctx->tctable_h.p) cudaFreeHost(ctx->tctable_h.p);
   for (auto& ev : ctx->prof_events) {
     cudaEventDestroy(ev.first);
     cudaEventDestroy(ev.second);

@@ -85,23 +85,32 @@ cudaError_t launch_reduce(const R* partial, size_t slice_stride, const int* coun
                           cudaStream_t st);
 
 // --- hv_tc.cu --------------------------------------------------------------
-struct TcLaunch {
-  const void* rec;      // SrcRec32 [nt][rec_stride], rewritten by launch_tc_relative
-  size_t rec_stride;    // records per time, a multiple of 32 >= nsrc
-  const int* counts;    // [nt]
-  int nsrc, nt, nf;
+// One simulation of a fused-kernel launch (device pointers).
+struct TcSimDesc {
+  const int* counts;    // [nt] sources above the horizon per time
   const void* U;        // Ucoef32 [nt][nf][Np]
   const float* beamT;   // [nf][P*P][Np]
-  int Np, nant, P;
   const float* umax;    // [nt * nf] bound of |U|_1 per slice (launch_ubound)
   float* partial;       // [nt * nf][ceil(nsrc / chunk)][2][Np][Np]
-  int chunk;            // sources per split-K chunk (multiple of 32)
-  const void* groups;   // device copy of the group table (tc_fill_group_table)
+  const void* groups;   // device group table (tc_fill_group_table for this nant)
   int ngroups, max_slots;
-  int* err;             // device error flag
-  int num_sms;
+  long long rec_row0;   // first record row of time 0 in the launch's record tensor
+  int rec_stride;       // records per time, a multiple of 32 >= nsrc
+  int nt, nf, Np, nant, P, nsrc;
+  int chunk;            // sources per split-K chunk (multiple of 32)
 };
-cudaError_t launch_tc(const TcLaunch& L, cudaStream_t st);
+size_t tc_sim_table_bytes(int nsims);
+int tc_num_groups(int nant);
+// One-time launch attributes of the fused kernel (call outside stream capture).
+cudaError_t tc_configure();
+// All items of nsims simulations in one persistent launch.  rec: SrcRec32
+// rows (rewritten by launch_tc_relative) of every simulation, rec_rows in
+// all.  d_table / h_table: device and host (kept alive until the copy ran)
+// buffers of tc_sim_table_bytes(nsims).  Cluster mode is used when every
+// simulation has the same clusterable group layout.
+cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, long long rec_rows,
+                            void* d_table, void* h_table, int* err, int num_sms,
+                            cudaStream_t st);
 size_t tc_partial_floats(int Np, int nsrc, int nslices, int chunk);
 int tc_chunk_sources(int nsrc, int nslices, int ngroups, int num_sms);
 size_t tc_group_table_bytes(int nant);
@@ -109,3 +118,9 @@ int tc_fill_group_table(int nant, void* host_buf);
 int tc_max_slots(int nant);
 
 }  // namespace hv
+
+// Context internals shared by the library's translation units (hv_api.cu).
+struct hv_context;
+cudaStream_t hv_context_stream(hv_context* ctx);
+void hv_context_set_error(hv_context* ctx, const char* msg);
+void hv_context_add_launches(hv_context* ctx, uint64_t n);

@@ -94,23 +94,35 @@ struct TcGroup {
   int write_mask;                      // CTAs this CTA's generators write to (bit = rank)
 };
 
+// One simulation of a launch.  A launch runs the items of every simulation
+// in its table; all of them share the record tensor (rows from rec_row0).
+struct TcSim {
+  const int* counts;      // [nt] sources above the horizon per time
+  const Ucoef32* U;       // [nt][nf][Np]
+  const float* beamT;     // [nf][PP][Np]
+  const float* umax;      // [nt * nf] bound of |U|_1 per slice
+  float* partial;         // [nt * nf][nchunk][2][Np][Np]
+  const TcGroup* groups;  // [ngroups]
+  long long item0;        // first item of this simulation in the launch
+  int rec_row0;           // first record row of time 0
+  int rec_stride;         // records per time (a multiple of 32)
+  int nt, nf, Np, PP, dx, dy;
+  int nchunk, chunk, ngroups;
+};
+
 struct TcParams {
-  const int* counts;    // [nt] sources above the horizon per time
-  int nsrc;             // catalogue size (bounds the split-K chunks)
-  int rec_stride;       // records per time in the record tensor
-  int nt, nf;           // times and frequencies of this launch
-  const Ucoef32* U;     // [nt][nf][Np]
-  const float* beamT;   // [nf][PP][Np]
-  const float* umax;    // [nt * nf] bound of |U|_1 per slice
-  int Np, nant, PP, dx, dy;
-  float* partial;       // [nt * nf][nchunk][2][Np][Np]
-  int nchunk, chunk;
-  const TcGroup* groups;
-  int ngroups;
+  const TcSim* sims;
+  int nsims;
+  long long total_items;
   int nstages, max_slots;
   int* err;
-  long long total_items;
 };
+
+// Read-only load of a pointer-valued field.
+template <typename T>
+__device__ __forceinline__ T* ldg_ptr(T* const* p) {
+  return reinterpret_cast<T*>(__ldg(reinterpret_cast<const unsigned long long*>(p)));
+}
 
 // ------------------------------------------------------------ PTX helpers --
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -479,31 +491,42 @@ __device__ __forceinline__ void gen_unit(const SrcRec32* rec, const Ucoef32& uc,
 
 // ------------------------------------------------------------- the kernel --
 struct ItemInfo {
+  const TcSim* sim;
   int g, k, tl, f, sl;
   int s0, s1, nst;
 };
 
-// Item it -> (group, chunk, slice).  Without clusters an item is one group of
-// one (slice, chunk); in cluster mode an item is a (slice, chunk) and every
-// CTA of the cluster takes its own group (its rank).
+// Item it -> (simulation, group, chunk, slice).  Without clusters an item is
+// one group of one (slice, chunk); in cluster mode an item is a (slice,
+// chunk) and every CTA of the cluster takes its own group (its rank).
 template <bool kCluster>
 __device__ __forceinline__ bool decode_item(const TcParams& p, long long it, int rank,
                                             ItemInfo& d) {
-  long long rest = it;
+  int lo = 0, hi = p.nsims - 1;  // last simulation with item0 <= it
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&p.sims[mid].item0) <= it) lo = mid;
+    else hi = mid - 1;
+  }
+  const TcSim* sm = p.sims + lo;
+  d.sim = sm;
+  long long rest = it - __ldg(&sm->item0);
+  const int ngroups = __ldg(&sm->ngroups), nchunk = __ldg(&sm->nchunk), nf = __ldg(&sm->nf);
   if (kCluster) {
     d.g = rank;
   } else {
-    d.g = (int)(it % p.ngroups);
-    rest = it / p.ngroups;
+    d.g = (int)(rest % ngroups);
+    rest = rest / ngroups;
   }
-  d.k = (int)(rest % p.nchunk);
-  d.sl = (int)(rest / p.nchunk);
-  d.tl = d.sl / p.nf;
-  d.f = d.sl % p.nf;
-  const int cnt = __ldg(p.counts + d.tl);
-  d.s0 = d.k * p.chunk;
+  d.k = (int)(rest % nchunk);
+  d.sl = (int)(rest / nchunk);
+  d.tl = d.sl / nf;
+  d.f = d.sl % nf;
+  const int cnt = __ldg(ldg_ptr(&sm->counts) + d.tl);
+  const int chunk = __ldg(&sm->chunk);
+  d.s0 = d.k * chunk;
   if (d.s0 >= cnt) return false;
-  d.s1 = min(d.s0 + p.chunk, cnt);
+  d.s1 = min(d.s0 + chunk, cnt);
   d.nst = (d.s1 - d.s0 + TC_KS - 1) / TC_KS;
   return true;
 }
@@ -537,9 +560,12 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int rank = kCluster ? (int)cluster_rank() : 0;
-  const long long it0 = kCluster ? blockIdx.x / p.ngroups : blockIdx.x;
-  const long long istep = kCluster ? gridDim.x / p.ngroups : gridDim.x;
-  const TcGroup* mine = p.groups + rank;  // cluster mode: this CTA's group
+  // cluster mode: every simulation of the launch has the same group layout
+  // (one group per CTA of the cluster), so its barrier counts are common
+  const int csize = kCluster ? (int)__ldg(&p.sims[0].ngroups) : 1;
+  const long long it0 = kCluster ? blockIdx.x / csize : blockIdx.x;
+  const long long istep = kCluster ? gridDim.x / csize : gridDim.x;
+  const TcGroup* mine = ldg_ptr(&p.sims[0].groups) + rank;
   // cluster mode: operand bytes this CTA receives from peers per stage
   const uint32_t recv_bytes = kCluster ? (uint32_t)__ldg(&mine->recv_slots) * TC_SLOT : 0u;
   if (threadIdx.x == 0) {
@@ -585,17 +611,19 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
     ItemInfo d;
     for (long long it = it0; it < p.total_items; it += istep) {
       if (!decode_item<kCluster>(p, it, rank, d)) continue;
-      const TcGroup* gp = p.groups + d.g;
+      const TcSim* sm = d.sim;
+      const TcGroup* gp = ldg_ptr(&sm->groups) + d.g;
+      const int Np = __ldg(&sm->Np), dx = __ldg(&sm->dx), dy = __ldg(&sm->dy);
       const int g_nslots = __ldg(&gp->nslots), g_npairs = __ldg(&gp->npairs);
       const int g_rows0 = __ldg(&gp->slot_rows[0]), g_rows1 = __ldg(&gp->slot_rows[1]),
                 g_rows2 = __ldg(&gp->slot_rows[2]);
       const int g_blk0 = __ldg(&gp->slot_block[0]), g_blk1 = __ldg(&gp->slot_block[1]),
                 g_blk2 = __ldg(&gp->slot_block[2]);
-      const Ucoef32* Us = p.U + (size_t)d.sl * p.Np;
-      const float umax_sl = __ldg(p.umax + d.sl);
+      const Ucoef32* Us = ldg_ptr(&sm->U) + (size_t)d.sl * Np;
+      const float umax_sl = __ldg(ldg_ptr(&sm->umax) + d.sl);
       if (umax_sl >= 4.0e6f && tid == 0) atomicExch(p.err, kErrRange);
       const float dlim = 8.0f / fmaxf(umax_sl, 1e-30f);
-      const float* beam = p.beamT + (size_t)d.f * p.PP * p.Np;
+      const float* beam = ldg_ptr(&sm->beamT) + (size_t)d.f * __ldg(&sm->PP) * Np;
       // the slots this CTA fills: all of its group's (no clusters) or the
       // ones it owns (cluster mode)
       const int nfill = kCluster ? nown : g_nslots;
@@ -637,7 +665,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
           uint4 re_h = make_uint4(0, 0, 0, 0), im_h = re_h, re_l = re_h, im_l = re_h;
           if (u_ok[i]) {
             float rv[8], iv[8];
-            gen_unit(recs + sg * 8, Us[u_a[i]], beam + u_a[i], p.Np, p.dx, p.dy, dlim, rv, iv);
+            gen_unit(recs + sg * 8, Us[u_a[i]], beam + u_a[i], Np, dx, dy, dlim, rv, iv);
             split_pack(rv, re_h, re_l);
             split_pack(iv, im_h, im_l);
           }
@@ -673,8 +701,8 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
         const int pr = cb >> 1, plane = cb & 1;
         if (pr < g_npairs) {
           const int I = __ldg(&gp->pI[pr]), J = __ldg(&gp->pJ[pr]);
-          float* out = p.partial +
-                       (((size_t)d.sl * p.nchunk + d.k) * 2 + plane) * (size_t)p.Np * p.Np;
+          float* out = ldg_ptr(&sm->partial) +
+                       (((size_t)d.sl * __ldg(&sm->nchunk) + d.k) * 2 + plane) * (size_t)Np * Np;
           const int a = I * TC_ROWS + q * 32 + lane;
 #pragma unroll 1
           for (int c32 = 0; c32 < 4; ++c32) {
@@ -682,7 +710,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
             tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cb * 128 + c32 * 32), v);
             const int b0 = J * TC_ROWS + c32 * 32;
 #pragma unroll
-            for (int c = 0; c < 32; ++c) out[(size_t)(b0 + c) * p.Np + a] = v[c];
+            for (int c = 0; c < 32; ++c) out[(size_t)(b0 + c) * Np + a] = v[c];
           }
         }
       }
@@ -705,7 +733,8 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
           if (!wait1(rec_empty(s), par ^ 1, abort_flag, p.err)) { ok = false; break; }
           mbar_expect_tx(rec_full(s), TC_REC);
           tma_load_2d(rec_base + (uint32_t)s * TC_REC, &rec_map, rec_full(s), 0,
-                      d.tl * p.rec_stride + d.s0 + j * TC_KS);
+                      __ldg(&d.sim->rec_row0) + d.tl * __ldg(&d.sim->rec_stride) + d.s0 +
+                          j * TC_KS);
         }
       }
       // let the copies still in flight land before the CTA can exit
@@ -721,7 +750,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
       const uint16_t cmask = kCluster ? (uint16_t)__ldg(&mine->commit_mask) : (uint16_t)1;
       for (long long it = it0; it < p.total_items && ok; it += istep) {
         if (!decode_item<kCluster>(p, it, rank, d)) continue;
-        const TcGroup* gp = p.groups + d.g;
+        const TcGroup* gp = ldg_ptr(&d.sim->groups) + d.g;
         const int n0 = __ldg(&gp->pN[0]), n1 = __ldg(&gp->pN[1]);
         const uint32_t idp0 = idesc_bf16(n0, false), idn0 = idesc_bf16(n0, true);
         const uint32_t idp1 = idesc_bf16(n1, false), idn1 = idesc_bf16(n1, true);
@@ -950,64 +979,99 @@ int tc_chunk_sources(int nsrc, int nslices, int ngroups, int num_sms) {
   return (int)c;
 }
 
-cudaError_t launch_tc(const TcLaunch& L, cudaStream_t st) {
-  if (L.nsrc <= 0 || L.nt <= 0) return cudaSuccess;
+size_t tc_sim_table_bytes(int nsims) { return sizeof(TcSim) * (size_t)std::max(nsims, 1); }
+
+cudaError_t tc_configure() {
+  static bool done = false;
+  if (done) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(tc_vis_kernel<false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_LIMIT);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(tc_vis_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           TC_SMEM_LIMIT);
+  if (e != cudaSuccess) return e;
+  done = true;
+  return cudaSuccess;
+}
+
+cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, long long rec_rows,
+                            void* d_table, void* h_table, int* err, int num_sms,
+                            cudaStream_t st) {
+  if (nsims <= 0 || rec_rows <= 0) return cudaSuccess;
   auto encode = encode_fn();
   if (!encode) return cudaErrorNotSupported;
   CUtensorMap map;
-  const cuuint64_t gdim[2] = {8, (cuuint64_t)L.nt * L.rec_stride};
+  const cuuint64_t gdim[2] = {8, (cuuint64_t)rec_rows};
   const cuuint64_t gstride[1] = {sizeof(SrcRec32)};
   const cuuint32_t box[2] = {8, TC_KS};
   const cuuint32_t estride[2] = {1, 1};
-  CUresult r = encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(L.rec), gdim,
+  CUresult r = encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(rec), gdim,
                       gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
                       CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
 
+  // cluster mode when every simulation has the same (clusterable) group layout
+  bool cluster = use_cluster(sims[0].ngroups);
+  int max_slots = 1;
+  for (int i = 0; i < nsims; ++i) {
+    if (sims[i].ngroups != sims[0].ngroups) cluster = false;
+    max_slots = std::max(max_slots, sims[i].max_slots);
+  }
+  TcSim* tab = static_cast<TcSim*>(h_table);
+  long long items = 0;
+  for (int i = 0; i < nsims; ++i) {
+    const TcSimDesc& L = sims[i];
+    TcSim t{};
+    t.counts = L.counts;
+    t.U = static_cast<const Ucoef32*>(L.U);
+    t.beamT = L.beamT;
+    t.umax = L.umax;
+    t.partial = L.partial;
+    t.groups = static_cast<const TcGroup*>(L.groups);
+    t.item0 = items;
+    t.rec_row0 = (int)L.rec_row0;
+    t.rec_stride = L.rec_stride;
+    t.nt = L.nt;
+    t.nf = L.nf;
+    t.Np = L.Np;
+    t.PP = L.P * L.P;
+    t.dx = L.P > 1 ? 1 : 0;
+    t.dy = L.P > 1 ? L.P : 0;
+    t.chunk = L.chunk;
+    t.nchunk = ceil_div(std::max(L.nsrc, 1), L.chunk);
+    t.ngroups = L.ngroups;
+    tab[i] = t;
+    items += (long long)L.nt * L.nf * t.nchunk * (cluster ? 1 : L.ngroups);
+  }
+  if (items == 0) return cudaSuccess;
+  cudaError_t e = cudaMemcpyAsync(d_table, h_table, sizeof(TcSim) * nsims, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+
   TcParams p{};
-  p.counts = L.counts;
-  p.nsrc = L.nsrc;
-  p.rec_stride = (int)L.rec_stride;
-  p.nt = L.nt;
-  p.nf = L.nf;
-  p.U = static_cast<const Ucoef32*>(L.U);
-  p.beamT = L.beamT;
-  p.umax = L.umax;
-  p.Np = L.Np;
-  p.nant = L.nant;
-  p.PP = L.P * L.P;
-  p.dx = L.P > 1 ? 1 : 0;
-  p.dy = L.P > 1 ? L.P : 0;
-  p.partial = L.partial;
-  p.chunk = L.chunk;
-  p.nchunk = ceil_div(L.nsrc, L.chunk);
-  p.groups = static_cast<const TcGroup*>(L.groups);
-  p.ngroups = L.ngroups;
-  p.max_slots = L.max_slots;
-  p.err = L.err;
-  p.total_items = (long long)L.nt * L.nf * p.nchunk * p.ngroups;
+  p.sims = static_cast<const TcSim*>(d_table);
+  p.nsims = nsims;
+  p.total_items = items;
+  p.max_slots = max_slots;
+  p.err = err;
   const int per_stage = p.max_slots * TC_SLOT + TC_REC;
   const int fixed = 1024 /*alignment*/ + 512 /*barriers, holder*/;
   p.nstages = std::min(4, (TC_SMEM_LIMIT - fixed) / per_stage);
   if (p.nstages < 2) return cudaErrorInvalidConfiguration;
   const int smem = fixed + p.nstages * per_stage;
-  cudaError_t e = cudaFuncSetAttribute(tc_vis_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       smem);
+  e = tc_configure();
   if (e != cudaSuccess) return e;
-  if (!use_cluster(p.ngroups)) {
-    const long long grid = std::min<long long>(L.num_sms, p.total_items);
+  if (!cluster) {
+    const long long grid = std::min<long long>(num_sms, items);
     tc_vis_kernel<false><<<(int)grid, TC_THREADS, smem, st>>>(map, p);
     return cudaGetLastError();
   }
   // cluster mode: one CTA per group, items are (slice, chunk)
-  p.total_items = (long long)L.nt * L.nf * p.nchunk;
-  e = cudaFuncSetAttribute(tc_vis_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return e;
+  const int C = sims[0].ngroups;
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = (unsigned)p.ngroups;
+  attr[0].val.clusterDim.x = (unsigned)C;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.blockDim = dim3(TC_THREADS);
@@ -1015,13 +1079,18 @@ cudaError_t launch_tc(const TcLaunch& L, cudaStream_t st) {
   cfg.stream = st;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cfg.gridDim = dim3((unsigned)(p.ngroups * (L.num_sms / p.ngroups)));
-  int nclusters = 0;
-  e = cudaOccupancyMaxActiveClusters(&nclusters, tc_vis_kernel<true>, &cfg);
-  if (e != cudaSuccess) return e;
+  cfg.gridDim = dim3((unsigned)(C * (num_sms / C)));
+  // co-resident clusters for this cluster size and shared memory (cached:
+  // the query is host-side and stays valid)
+  static int cached_n[TC_MAX_CLUSTER + 1][5] = {};
+  int& nclusters = cached_n[C][p.nstages];
+  if (nclusters == 0) {
+    e = cudaOccupancyMaxActiveClusters(&nclusters, tc_vis_kernel<true>, &cfg);
+    if (e != cudaSuccess) return e;
+  }
   if (nclusters < 1) return cudaErrorInvalidConfiguration;
-  nclusters = (int)std::min<long long>(nclusters, p.total_items);
-  cfg.gridDim = dim3((unsigned)(p.ngroups * nclusters));
+  const int ncl = (int)std::min<long long>(nclusters, items);
+  cfg.gridDim = dim3((unsigned)(C * ncl));
   e = cudaLaunchKernelEx(&cfg, tc_vis_kernel<true>, map, p);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();

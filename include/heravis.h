@@ -117,6 +117,46 @@ int hv_sync(hv_context* ctx);
 int hv_set_profiling(hv_context* ctx, int enable);
 int hv_profile_read(hv_context* ctx, double* ms, uint64_t* launches);
 
+/* ---- batched form -------------------------------------------------------
+ * Many independent simulations (precision 1, fused tensor-core form) planned
+ * and run together: the reference's per-call vis_gpu (vis.py:144-262) applied
+ * to a list of (layout, sky, beams, frequencies) without a host loop.  Every
+ * array of an hv_sim is in device memory except `freqs` (host, copied at
+ * plan time); the output is (nfreq, ntimes, nant, nant) complex64. */
+typedef struct {
+  const float* antpos;    /* (nant, 3)            */
+  const float* eq2tops;   /* (ntimes, 3, 3)       */
+  const float* crd_eq;    /* (3, nsrc)            */
+  const float* I_sky;     /* (nsrc,)              */
+  const float* bm_cubes;  /* (nfreq, nant, P, P)  */
+  const double* freqs;    /* (nfreq,) host, Hz    */
+  void* vis_out;          /* (nfreq, ntimes, nant, nant) complex64 */
+  int nant, ntimes, nsrc, nfreq, beam_px;
+} hv_sim;
+
+typedef struct hv_batch hv_batch;
+
+enum {
+  HV_BATCH_GRAPH = 1,     /* capture the batch into a CUDA graph at creation  */
+  HV_BATCH_AUTOTUNE = 2   /* time split-K depths per cluster class, keep best */
+};
+
+/* Plan a batch on the context's device: one workspace for all simulations,
+ * one persistent fused launch per cluster class.  The hv_sim arrays must
+ * stay at the same addresses for the life of the batch (a graph replays
+ * them).  Runs the batch once when autotuning. */
+int hv_batch_create(hv_context* ctx, const hv_sim* sims, int nsims, unsigned flags,
+                    hv_batch** batch);
+/* Enqueue one run of the batch on `stream` (NULL = the context's stream). */
+int hv_batch_launch(hv_batch* batch, void* stream);
+/* Wait for the device and report a device-side error of the batch. */
+int hv_batch_sync(hv_batch* batch);
+/* Kernel launches in one run of the batch. */
+uint64_t hv_batch_launches(const hv_batch* batch);
+int hv_batch_destroy(hv_batch* batch);
+/* Plan, run once, wait, free. */
+int hv_vis_batch(hv_context* ctx, const hv_sim* sims, int nsims, void* stream);
+
 /* No counterpart in the reference: an entry point for callers that cannot
  * allocate device memory when they ask for visibilities (a real-time
  * pipeline whose device memory is fixed before it starts, or a framework
