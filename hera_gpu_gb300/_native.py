@@ -64,6 +64,10 @@ SIGNATURES = {
     "hv_batch_launches": (ctypes.c_uint64, [_c_void_p]),
     "hv_batch_destroy": (_c_int, [_c_void_p]),
     "hv_vis_batch": (_c_int, [_c_void_p, ctypes.POINTER(HvSim), _c_int, _c_void_p]),
+    "hv_device_alloc": (_c_int, [_c_void_p, _c_size_t, ctypes.POINTER(_c_void_p)]),
+    "hv_device_free": (_c_int, [_c_void_p, _c_void_p]),
+    "hv_memcpy_async": (_c_int, [_c_void_p, _c_void_p, _c_void_p, _c_size_t, _c_int]),
+    "hv_stream_query": (_c_int, [_c_void_p]),
     "hv_host_alloc": (_c_int, [_c_void_p, _c_size_t, ctypes.POINTER(_c_void_p)]),
     "hv_host_free": (_c_int, [_c_void_p, _c_void_p]),
 }
@@ -176,6 +180,29 @@ class Context:
             ctypes.c_void_p(d_bm_cubes), int(beam_px), ctypes.c_void_p(d_out),
             ctypes.c_void_p(stream))
         self.check(rc)
+
+    def device_alloc(self, nbytes: int) -> int:
+        p = ctypes.c_void_p()
+        self.check(self.lib.hv_device_alloc(self.h, int(nbytes), ctypes.byref(p)))
+        return int(p.value or 0)
+
+    def device_free(self, ptr: int):
+        self.check(self.lib.hv_device_free(self.h, ctypes.c_void_p(ptr)))
+
+    def h2d(self, dst: int, src: np.ndarray):
+        """Asynchronous copy on the context's stream (src must stay alive
+        until the stream has passed it; page-locked for true overlap)."""
+        self.check(self.lib.hv_memcpy_async(self.h, ctypes.c_void_p(dst), _ptr(src), src.nbytes, 1))
+
+    def d2h(self, dst: np.ndarray, src: int):
+        self.check(self.lib.hv_memcpy_async(self.h, _ptr(dst), ctypes.c_void_p(src), dst.nbytes, 2))
+
+    def idle(self) -> bool:
+        """True once all work queued on the context's stream has finished."""
+        r = self.lib.hv_stream_query(self.h)
+        if r < 0:
+            self.check(-r)
+        return r == 0
 
     def set_profiling(self, enable: bool):
         self.check(self.lib.hv_set_profiling(self.h, 1 if enable else 0))

@@ -374,6 +374,12 @@ int hv_create(hv_context** out, int device, size_t hbm_budget_bytes) {
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { r = HV_ERR_CUDA; break; }
     if (cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess) { r = HV_ERR_OOM; break; }
     if (cudaMemset(ctx->d_err, 0, sizeof(int)) != cudaSuccess) { r = HV_ERR_CUDA; break; }
+    // keep freed stream-ordered memory in the pool for reuse
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+      uint64_t keep = ~0ull;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
   } while (0);
   if (r != HV_OK) {
     cudaGetLastError();
@@ -502,6 +508,41 @@ int hv_profile_read(hv_context* ctx, double* ms, uint64_t* launches) {
   }
   ctx->prof_events.clear();
   return HV_OK;
+}
+
+int hv_device_alloc(hv_context* ctx, size_t bytes, void** ptr) {
+  if (!ctx || !ptr) return HV_ERR_ARG;
+  HV_CK(cudaSetDevice(ctx->device));
+  cudaError_t e = cudaMallocAsync(ptr, bytes ? bytes : 1, ctx->stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, HV_ERR_OOM, "cudaMallocAsync(%zu) failed: %s", bytes, cudaGetErrorString(e));
+  }
+  return HV_OK;
+}
+
+int hv_device_free(hv_context* ctx, void* ptr) {
+  if (!ctx) return HV_ERR_ARG;
+  if (ptr) HV_CK(cudaFreeAsync(ptr, ctx->stream));
+  return HV_OK;
+}
+
+int hv_memcpy_async(hv_context* ctx, void* dst, const void* src, size_t bytes, int kind) {
+  if (!ctx || (bytes && (!dst || !src)) || kind < 1 || kind > 3) return HV_ERR_ARG;
+  if (!bytes) return HV_OK;
+  const cudaMemcpyKind k = kind == 1 ? cudaMemcpyHostToDevice
+                           : kind == 2 ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  HV_CK(cudaMemcpyAsync(dst, src, bytes, k, ctx->stream));
+  return HV_OK;
+}
+
+int hv_stream_query(hv_context* ctx) {
+  if (!ctx) return -HV_ERR_ARG;
+  const cudaError_t e = cudaStreamQuery(ctx->stream);
+  if (e == cudaSuccess) return 0;
+  if (e == cudaErrorNotReady) return 1;
+  ctx->err = cudaGetErrorString(e);
+  return -HV_ERR_CUDA;
 }
 
 int hv_host_alloc(hv_context* ctx, size_t bytes, void** ptr) {

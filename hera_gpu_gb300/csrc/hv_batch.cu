@@ -138,15 +138,28 @@ void layout(hv_batch* b) {
   b->host_bytes = hoff + up256(hv::tc_sim_table_bytes((int)(b->sims.size() + b->classes.size())));
 }
 
+// Device memory of the batch comes from the stream-ordered pool of the
+// context's stream: creating and destroying batches does not stall work on
+// other streams.
+void release(hv_batch* b) {
+  cudaStream_t st = hv_context_stream(b->ctx);
+  if (b->arena) cudaFreeAsync(b->arena, st);
+  if (b->rec) cudaFreeAsync(b->rec, st);
+  if (b->table) cudaFreeAsync(b->table, st);
+  b->arena = b->rec = b->table = nullptr;
+}
+
 int allocate(hv_batch* b) {
-  if (b->arena) cudaFree(b->arena);
-  if (b->rec) cudaFree(b->rec);
-  if (b->table) cudaFree(b->table);
-  if (b->host) cudaFreeHost(b->host);
-  b->arena = b->rec = b->table = b->host = nullptr;
-  HB_CK(cudaMalloc(&b->arena, std::max<size_t>(b->arena_bytes, 256)));
-  HB_CK(cudaMalloc(&b->rec, sizeof(hv::SrcRec32) * (size_t)std::max<long long>(b->rec_rows, 1)));
-  HB_CK(cudaMalloc(&b->table, hv::tc_sim_table_bytes((int)(b->sims.size() + b->classes.size()))));
+  cudaStream_t st = hv_context_stream(b->ctx);
+  release(b);
+  if (b->host) {
+    cudaStreamSynchronize(st);  // the host block may still feed queued copies
+    cudaFreeHost(b->host);
+  }
+  b->host = nullptr;
+  HB_CK(cudaMallocAsync(&b->arena, std::max<size_t>(b->arena_bytes, 256), st));
+  HB_CK(cudaMallocAsync(&b->rec, sizeof(hv::SrcRec32) * (size_t)std::max<long long>(b->rec_rows, 1), st));
+  HB_CK(cudaMallocAsync(&b->table, hv::tc_sim_table_bytes((int)(b->sims.size() + b->classes.size())), st));
   HB_CK(cudaHostAlloc(&b->host, std::max<size_t>(b->host_bytes, 256), cudaHostAllocDefault));
   // constant host data: frequencies and group tables
   char* h = static_cast<char*>(b->host);
@@ -282,8 +295,9 @@ int hv_batch_create(hv_context* ctx, const hv_sim* sims, int nsims, unsigned fla
     cudaDeviceProp prop;
     if (cudaGetDeviceProperties(&prop, b->device) != cudaSuccess) { r = HV_ERR_CUDA; break; }
     b->num_sms = prop.multiProcessorCount;
-    if (cudaMalloc(&b->d_err, sizeof(int)) != cudaSuccess) { r = HV_ERR_OOM; break; }
-    cudaMemset(b->d_err, 0, sizeof(int));
+    if (cudaMallocAsync(reinterpret_cast<void**>(&b->d_err), sizeof(int), hv_context_stream(ctx)) !=
+        cudaSuccess) { r = HV_ERR_OOM; break; }
+    cudaMemsetAsync(b->d_err, 0, sizeof(int), hv_context_stream(ctx));
     std::map<int, int> class_of;  // cluster size (0 = no cluster) -> class
     for (int i = 0; i < nsims; ++i) {
       r = check_sim(b, sims[i], i);
@@ -361,6 +375,8 @@ int hv_batch_create(hv_context* ctx, const hv_sim* sims, int nsims, unsigned fla
       b->graph = g;
       if (cudaGraphInstantiate(&b->exec, g, 0) != cudaSuccess) { r = HV_ERR_CUDA; break; }
     }
+    // allocations and constant copies done before the batch may run elsewhere
+    if (cudaStreamSynchronize(st) != cudaSuccess) { r = HV_ERR_CUDA; break; }
   } while (0);
   if (r != HV_OK) {
     if (ctx) hv_context_set_error(ctx, b->err.empty() ? "hv_batch_create failed" : b->err.c_str());
@@ -390,7 +406,7 @@ int hv_batch_launch(hv_batch* b, void* stream) {
 
 int hv_batch_sync(hv_batch* b) {
   if (!b) return HV_ERR_ARG;
-  if (cudaDeviceSynchronize() != cudaSuccess) return HV_ERR_CUDA;
+  if (cudaStreamSynchronize(hv_context_stream(b->ctx)) != cudaSuccess) return HV_ERR_CUDA;
   int flag = 0;
   if (cudaMemcpy(&flag, b->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
     return HV_ERR_CUDA;
@@ -405,14 +421,16 @@ uint64_t hv_batch_launches(const hv_batch* b) { return b ? b->launches_per_run :
 
 int hv_batch_destroy(hv_batch* b) {
   if (!b) return HV_OK;
-  cudaDeviceSynchronize();
+  // runs of the batch are ordered on the context's stream (or were waited
+  // for by the caller): release after them
+  if (b->ctx) {
+    cudaStreamSynchronize(hv_context_stream(b->ctx));
+    release(b);
+  }
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
-  if (b->arena) cudaFree(b->arena);
-  if (b->rec) cudaFree(b->rec);
-  if (b->table) cudaFree(b->table);
   if (b->host) cudaFreeHost(b->host);
-  if (b->d_err) cudaFree(b->d_err);
+  if (b->d_err) cudaFreeAsync(b->d_err, hv_context_stream(b->ctx));
   delete b;
   return HV_OK;
 }

@@ -177,6 +177,17 @@ int hv_vis_gpu_noalloc(const void* d_antpos, int nant, double freq,
                        const void* d_bm_cube, int beam_px, void* d_vis_out,
                        void* stream, char* errbuf, size_t errlen);
 
+/* Device memory and copies ordered on the context's stream (stream-ordered
+ * allocation, so freeing does not stall other streams); used by host code
+ * that keeps inputs resident or serves requests.  kind: 1 host->device,
+ * 2 device->host, 3 device->device. */
+int hv_device_alloc(hv_context* ctx, size_t bytes, void** ptr);
+int hv_device_free(hv_context* ctx, void* ptr);
+int hv_memcpy_async(hv_context* ctx, void* dst, const void* src, size_t bytes, int kind);
+/* 0 when every operation queued on the context's stream has finished, 1 while
+ * work is pending; a negative hv_status on error. */
+int hv_stream_query(hv_context* ctx);
+
 /* Page-locked host memory for fast host<->device copies (cudaHostAlloc). */
 int hv_host_alloc(hv_context* ctx, size_t bytes, void** ptr);
 int hv_host_free(hv_context* ctx, void* ptr);
