@@ -56,6 +56,9 @@ def parse_args():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=400,
+                    help="requests of the serving leg (0 = skip)")
+    ap.add_argument("--serve-rate", type=float, default=200.0)
     return ap.parse_args()
 
 
@@ -446,7 +449,6 @@ def run_ours(args):
     # ---- CPU baseline on a bounded sample, and the error of that sample ----
     if rank == 0 and pool is not None:
         V_cpu, wall, nsamp = cpu_sample(pool, cores, w, 0, 0)
-        pool.close()
         line["cpu_baseline"] = {
             "value": cpu_rate(wall, nsamp, N, S), "unit": "vis/s", "cores": cores,
             "kind": "port",
@@ -460,11 +462,67 @@ def run_ours(args):
             errs[method] = float(np.linalg.norm(v - V_cpu) / np.linalg.norm(V_cpu))
         line["rel_err_vs_fp64"] = {**errs, "sample": f"{N} ant x {nsamp} src, one slice"}
 
+    # ---- serving: Poisson request stream, continuous batching --------------
+    if rank == 0 and args.serve_requests > 0:
+        line["serve"] = run_serve(args, local, pool)
+
+    if pool is not None:
+        pool.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def run_serve(args, device, pool):
+    """The serving configuration: Poisson arrivals at --serve-rate of requests
+    from the batched-form size distribution plus 5 % large requests (350
+    antennas, 1M sources, 60 LSTs), 8 resident beam/layout sets, HBM budget
+    150 GB, 4 slots.  Latency = arrival to result in host memory."""
+    import numpy as np
+    from hera_gpu_gb300 import _native, serve
+    specs, reqs = serve.workload(args.serve_requests, rate_hz=args.serve_rate, seed=7)
+    ctxs = [_native.Context(device) for _ in range(4)]
+    sets = serve.build_sets(ctxs[0], specs, nfreq=16)
+    # warm the plan/launch path once (first-use costs are not steady state)
+    warm = serve.workload(4, rate_hz=1e4, large_frac=0.0, seed=99)[1]
+    for r in warm:
+        r.set_id = r.set_id % len(sets)
+    srv = serve.Server(sets, ctxs, hbm_budget=150e9, max_batch=32)
+    srv.run(warm)
+    done = srv.run(reqs)
+    wall = max(r.t_done for r in done)
+    out = serve.summarize(done, wall)
+    out.update({"rate_hz": args.serve_rate, "large_frac": 0.05, "slots": len(ctxs),
+                "resident_sets": len(sets), "hbm_budget_gb": 150,
+                "latency": "arrival to result in host memory"})
+    # error vs the FP64 oracle on a 1 % sample (one (time, channel) slice of
+    # each sampled small request; the checker runs in the host-process pool)
+    if pool is not None:
+        rng = np.random.default_rng(3)
+        small = [r for r in done if r.nsrc < 100_000]
+        pick = rng.choice(len(small), size=max(1, len(done) // 100), replace=False)
+        errs = []
+        for k in pick:
+            r = small[k]
+            sp = specs[r.set_id]
+            g = np.random.default_rng(sp["seed"])
+            full = serve.synth.hex_array(350, 14.6, 0.01, g)
+            sel = np.sort(g.choice(350, size=sp["nant"], replace=False))
+            dish = 14.0 * (1.0 + 0.02 * g.uniform(-1.0, 1.0, sp["nant"]))
+            f0 = sets[r.set_id].freqs[0]
+            bm = serve.synth.airy_beams(sp["nant"], sp["P"], f0, dish).astype(np.float32)
+            ant = full[sel].astype(np.float32).astype(np.float64)
+            V = pool.apply(_cpu_worker, ((ant, float(f0), r.eq2tops[0].astype(np.float64),
+                                          r.crd_eq.astype(np.float64),
+                                          r.I_sky.astype(np.float64), bm),))[0]
+            errs.append(float(np.linalg.norm(r.result[0, 0] - V) / max(np.linalg.norm(V), 1e-300)))
+        out["sample_rel_err_max"] = max(errs)
+        out["sample"] = f"{len(errs)} requests, slice (t=0, {sets[0].freqs[0] / 1e6:.0f} MHz)"
+    for st in sets:
+        st.close()
+    return out
 
 
 def main():

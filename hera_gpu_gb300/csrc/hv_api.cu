@@ -56,6 +56,9 @@ struct hv_context {
   DevBuf freqs, beamT, ucoef, rec, counts, blkcounts, v, partial, tcgroups;
   DevBuf umax, sortkv, crd_sorted, I_sorted, tctable;
   HostBuf tctable_h;  // page-locked staging of the fused kernel's simulation table
+  // page-locked blocks given back by destroyed batches, kept for the next
+  // ones: freeing page-locked memory waits for the whole device
+  std::vector<std::pair<void*, size_t>> host_pool;
 };
 
 namespace {
@@ -345,6 +348,40 @@ int check_err_flag(hv_context* ctx) {
 cudaStream_t hv_context_stream(hv_context* ctx) { return ctx->stream; }
 void hv_context_set_error(hv_context* ctx, const char* msg) { ctx->err = msg; }
 void hv_context_add_launches(hv_context* ctx, uint64_t n) { ctx->launches += n; }
+int hv_context_num_sms(hv_context* ctx) { return ctx->num_sms; }
+
+void* hv_context_host_take(hv_context* ctx, size_t bytes, size_t* cap) {
+  // the smallest pooled block that fits, else a new one
+  size_t best = ctx->host_pool.size();
+  for (size_t i = 0; i < ctx->host_pool.size(); ++i)
+    if (ctx->host_pool[i].second >= bytes &&
+        (best == ctx->host_pool.size() || ctx->host_pool[i].second < ctx->host_pool[best].second))
+      best = i;
+  if (best < ctx->host_pool.size()) {
+    void* p = ctx->host_pool[best].first;
+    *cap = ctx->host_pool[best].second;
+    ctx->host_pool.erase(ctx->host_pool.begin() + (long)best);
+    return p;
+  }
+  const size_t want = std::max<size_t>(4096, bytes + bytes / 4);
+  void* p = nullptr;
+  if (cudaHostAlloc(&p, want, cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  *cap = want;
+  return p;
+}
+
+void hv_context_host_give(hv_context* ctx, void* p, size_t cap) {
+  if (p) ctx->host_pool.emplace_back(p, cap);
+}
+
+void hv_context_record_kernel(hv_context* ctx, cudaEvent_t e0, cudaEvent_t e1) {
+  ctx->prof_events.emplace_back(e0, e1);
+}
+
+bool hv_context_profiling(hv_context* ctx) { return ctx->profiling; }
 
 extern "C" {
 
@@ -400,6 +437,7 @@ int hv_destroy(hv_context* ctx) {
                     &ctx->umax, &ctx->sortkv, &ctx->crd_sorted, &ctx->I_sorted, &ctx->tctable};
   for (DevBuf* b : bufs) release(ctx, *b);
   if (ctx->tctable_h.p) cudaFreeHost(ctx->tctable_h.p);
+  for (auto& hp : ctx->host_pool) cudaFreeHost(hp.first);
   for (auto& ev : ctx->prof_events) {
     cudaEventDestroy(ev.first);
     cudaEventDestroy(ev.second);

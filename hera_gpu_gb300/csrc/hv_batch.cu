@@ -58,6 +58,7 @@ struct hv_batch {
   long long rec_rows = 0;
   void* table = nullptr;                   // device simulation tables, per class
   void* host = nullptr;                    // pinned: frequencies, group tables, sim tables
+  size_t host_cap = 0;                     // its size (a block of the context's pool)
   size_t host_bytes = 0, h_table = 0, h_groups = 0;
   int* d_err = nullptr;
   cudaGraph_t graph = nullptr;
@@ -87,6 +88,20 @@ int bfail(hv_batch* b, int code, const char* fmt, ...) {
 
 int rec_stride_of(int nsrc) { return ((std::max(nsrc, 1) + 31) / 32) * 32; }
 
+// Split-K of a batch: a slice's sources are cut into chunks of at most
+// kBatchChunk (divided further by the class's autotuned divisor), so that
+// one item of the persistent launch stays within a few milliseconds and a
+// large simulation spreads over every SM.  The cut depends on the
+// simulation alone: its result does not depend on the batch it runs in.
+constexpr int kBatchChunk = 65536;
+
+void chunking(int nsrc, int div, int* chunk, int* nchunk) {
+  const int S = std::max(nsrc, 1);
+  const int parts = hv::ceil_div(S, kBatchChunk) * std::max(div, 1);
+  *chunk = std::max(32, hv::ceil_div(hv::ceil_div(S, parts), 32) * 32);
+  *nchunk = hv::ceil_div(S, *chunk);
+}
+
 // Lay out every simulation in the arena (split-K depth from the class divisor).
 void layout(hv_batch* b) {
   size_t off = 0, hoff = 0;
@@ -96,11 +111,8 @@ void layout(hv_batch* b) {
     const hv_sim& in = s.in;
     const int T = in.ntimes, F = in.nfreq, S = in.nsrc, P = in.beam_px;
     s.Np = hv::ceil_div(in.nant, hv::kAntPad) * hv::kAntPad;
-    // one chunk per slice by default: a batch has items enough in its slices
     const int div = b->class_nchunk_div.empty() ? 1 : b->class_nchunk_div[s.cls];
-    const int up_est = std::max(1, S);
-    s.chunk = std::max(32, ((up_est / div + 31) / 32) * 32);
-    s.nchunk = hv::ceil_div(std::max(S, 1), s.chunk);
+    chunking(S, div, &s.chunk, &s.nchunk);
     s.rec_stride = rec_stride_of(S);
     s.rec_row0 = rows;
     rows += (long long)T * s.rec_stride;
@@ -152,15 +164,18 @@ void release(hv_batch* b) {
 int allocate(hv_batch* b) {
   cudaStream_t st = hv_context_stream(b->ctx);
   release(b);
-  if (b->host) {
+  if (b->host && b->host_cap < b->host_bytes) {
     cudaStreamSynchronize(st);  // the host block may still feed queued copies
-    cudaFreeHost(b->host);
+    hv_context_host_give(b->ctx, b->host, b->host_cap);
+    b->host = nullptr;
   }
-  b->host = nullptr;
   HB_CK(cudaMallocAsync(&b->arena, std::max<size_t>(b->arena_bytes, 256), st));
   HB_CK(cudaMallocAsync(&b->rec, sizeof(hv::SrcRec32) * (size_t)std::max<long long>(b->rec_rows, 1), st));
   HB_CK(cudaMallocAsync(&b->table, hv::tc_sim_table_bytes((int)(b->sims.size() + b->classes.size())), st));
-  HB_CK(cudaHostAlloc(&b->host, std::max<size_t>(b->host_bytes, 256), cudaHostAllocDefault));
+  if (!b->host) {
+    b->host = hv_context_host_take(b->ctx, std::max<size_t>(b->host_bytes, 256), &b->host_cap);
+    if (!b->host) return bfail(b, HV_ERR_OOM, "page-locked host block of %zu bytes", b->host_bytes);
+  }
   // constant host data: frequencies and group tables
   char* h = static_cast<char*>(b->host);
   for (auto& s : b->sims) {
@@ -218,11 +233,18 @@ int enqueue(hv_batch* b, cudaStream_t st, int timed_class = -1) {
       nl += 3;
     }
   }
-  // one persistent fused launch per class
+  // one persistent fused launch per class; its items are handed out
+  // round-robin in table order, so the simulations with the largest items
+  // go first and the small ones fill the tail
   size_t toff = 0;
   for (size_t c = 0; c < b->classes.size(); ++c) {
+    std::vector<int> order = b->classes[c];
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+      const SimPlan &sx = b->sims[x], &sy = b->sims[y];
+      return std::min(sx.chunk, sx.in.nsrc) > std::min(sy.chunk, sy.in.nsrc);
+    });
     std::vector<TcSimDesc> d;
-    for (int i : b->classes[c]) {
+    for (int i : order) {
       const SimPlan& s = b->sims[i];
       if (s.in.ntimes == 0 || s.in.nsrc == 0) continue;
       TcSimDesc x{};
@@ -246,9 +268,23 @@ int enqueue(hv_batch* b, cudaStream_t st, int timed_class = -1) {
       d.push_back(x);
     }
     if (!d.empty() && (timed_class < 0 || timed_class == (int)c)) {
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      const bool prof = timed_class < 0 && hv_context_profiling(b->ctx) &&
+                        cudaStreamIsCapturing(st, &cs) == cudaSuccess &&
+                        cs == cudaStreamCaptureStatusNone;
+      if (prof) {
+        HB_CK(cudaEventCreate(&e0));
+        HB_CK(cudaEventCreate(&e1));
+        HB_CK(cudaEventRecord(e0, st));
+      }
       HB_CK(launch_tc_batch(d.data(), (int)d.size(), b->rec, b->rec_rows,
                             static_cast<char*>(b->table) + toff, H + b->h_table + toff, b->d_err,
                             b->num_sms, st));
+      if (prof) {
+        HB_CK(cudaEventRecord(e1, st));
+        hv_context_record_kernel(b->ctx, e0, e1);
+      }
       ++nl;
     }
     toff += tc_sim_table_bytes((int)d.size());
@@ -292,9 +328,7 @@ int hv_batch_create(hv_context* ctx, const hv_sim* sims, int nsims, unsigned fla
   int r = HV_OK;
   do {
     if (cudaGetDevice(&b->device) != cudaSuccess) { r = HV_ERR_CUDA; break; }
-    cudaDeviceProp prop;
-    if (cudaGetDeviceProperties(&prop, b->device) != cudaSuccess) { r = HV_ERR_CUDA; break; }
-    b->num_sms = prop.multiProcessorCount;
+    b->num_sms = hv_context_num_sms(ctx);
     if (cudaMallocAsync(reinterpret_cast<void**>(&b->d_err), sizeof(int), hv_context_stream(ctx)) !=
         cudaSuccess) { r = HV_ERR_OOM; break; }
     cudaMemsetAsync(b->d_err, 0, sizeof(int), hv_context_stream(ctx));
@@ -429,7 +463,7 @@ int hv_batch_destroy(hv_batch* b) {
   }
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
-  if (b->host) cudaFreeHost(b->host);
+  if (b->host) hv_context_host_give(b->ctx, b->host, b->host_cap);
   if (b->d_err) cudaFreeAsync(b->d_err, hv_context_stream(b->ctx));
   delete b;
   return HV_OK;

@@ -124,3 +124,12 @@ struct hv_context;
 cudaStream_t hv_context_stream(hv_context* ctx);
 void hv_context_set_error(hv_context* ctx, const char* msg);
 void hv_context_add_launches(hv_context* ctx, uint64_t n);
+int hv_context_num_sms(hv_context* ctx);
+// Page-locked host block of at least `bytes` (its size in *cap) from the
+// context's pool of returned blocks, or newly allocated; nullptr on failure.
+void* hv_context_host_take(hv_context* ctx, size_t bytes, size_t* cap);
+// Returns a block to the pool (no copy may still read it).
+void hv_context_host_give(hv_context* ctx, void* p, size_t cap);
+// Profiling: the context owns and times the pair of recorded events.
+bool hv_context_profiling(hv_context* ctx);
+void hv_context_record_kernel(hv_context* ctx, cudaEvent_t e0, cudaEvent_t e1);

@@ -110,8 +110,13 @@ struct TcSim {
   int nchunk, chunk, ngroups;
 };
 
+// A launch of one simulation carries its entry in the kernel parameters
+// (kTable = false: the fields are constant-bank operands and hold no
+// registers in the generator loop); a batched launch reads the table in
+// global memory.
 struct TcParams {
   const TcSim* sims;
+  TcSim one;
   int nsims;
   long long total_items;
   int nstages, max_slots;
@@ -499,19 +504,25 @@ struct ItemInfo {
 // Item it -> (simulation, group, chunk, slice).  Without clusters an item is
 // one group of one (slice, chunk); in cluster mode an item is a (slice,
 // chunk) and every CTA of the cluster takes its own group (its rank).
-template <bool kCluster>
+// Field f of the item's simulation (d: its ItemInfo).
+#define SIM_I(d, f) (kTable ? __ldg(&(d).sim->f) : p.one.f)
+#define SIM_P(d, f) (kTable ? ldg_ptr(&(d).sim->f) : p.one.f)
+
+template <bool kCluster, bool kTable>
 __device__ __forceinline__ bool decode_item(const TcParams& p, long long it, int rank,
                                             ItemInfo& d) {
-  int lo = 0, hi = p.nsims - 1;  // last simulation with item0 <= it
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (__ldg(&p.sims[mid].item0) <= it) lo = mid;
-    else hi = mid - 1;
+  long long rest = it;
+  if (kTable) {
+    int lo = 0, hi = p.nsims - 1;  // last simulation with item0 <= it
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(&p.sims[mid].item0) <= it) lo = mid;
+      else hi = mid - 1;
+    }
+    d.sim = p.sims + lo;
+    rest -= __ldg(&d.sim->item0);
   }
-  const TcSim* sm = p.sims + lo;
-  d.sim = sm;
-  long long rest = it - __ldg(&sm->item0);
-  const int ngroups = __ldg(&sm->ngroups), nchunk = __ldg(&sm->nchunk), nf = __ldg(&sm->nf);
+  const int ngroups = SIM_I(d, ngroups), nchunk = SIM_I(d, nchunk), nf = SIM_I(d, nf);
   if (kCluster) {
     d.g = rank;
   } else {
@@ -522,8 +533,8 @@ __device__ __forceinline__ bool decode_item(const TcParams& p, long long it, int
   d.sl = (int)(rest / nchunk);
   d.tl = d.sl / nf;
   d.f = d.sl % nf;
-  const int cnt = __ldg(ldg_ptr(&sm->counts) + d.tl);
-  const int chunk = __ldg(&sm->chunk);
+  const int cnt = __ldg(SIM_P(d, counts) + d.tl);
+  const int chunk = SIM_I(d, chunk);
   d.s0 = d.k * chunk;
   if (d.s0 >= cnt) return false;
   d.s1 = min(d.s0 + chunk, cnt);
@@ -533,9 +544,9 @@ __device__ __forceinline__ bool decode_item(const TcParams& p, long long it, int
 
 // 18 warps on 4 schedulers: the busiest scheduler holds 5 warps, and its
 // 16K-register file caps a thread at 96 registers (launch bounds give that).
-template <bool kCluster>
+template <bool kCluster, bool kTable>
 __global__ void __launch_bounds__(TC_THREADS, 1)
-tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
+tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant__ TcParams p) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
@@ -562,10 +573,10 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
   const int rank = kCluster ? (int)cluster_rank() : 0;
   // cluster mode: every simulation of the launch has the same group layout
   // (one group per CTA of the cluster), so its barrier counts are common
-  const int csize = kCluster ? (int)__ldg(&p.sims[0].ngroups) : 1;
+  const int csize = kCluster ? (kTable ? (int)__ldg(&p.sims[0].ngroups) : p.one.ngroups) : 1;
   const long long it0 = kCluster ? blockIdx.x / csize : blockIdx.x;
   const long long istep = kCluster ? gridDim.x / csize : gridDim.x;
-  const TcGroup* mine = ldg_ptr(&p.sims[0].groups) + rank;
+  const TcGroup* mine = (kTable ? ldg_ptr(&p.sims[0].groups) : p.one.groups) + rank;
   // cluster mode: operand bytes this CTA receives from peers per stage
   const uint32_t recv_bytes = kCluster ? (uint32_t)__ldg(&mine->recv_slots) * TC_SLOT : 0u;
   if (threadIdx.x == 0) {
@@ -610,20 +621,19 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
     uint32_t gs = 0, ic = 0;
     ItemInfo d;
     for (long long it = it0; it < p.total_items; it += istep) {
-      if (!decode_item<kCluster>(p, it, rank, d)) continue;
-      const TcSim* sm = d.sim;
-      const TcGroup* gp = ldg_ptr(&sm->groups) + d.g;
-      const int Np = __ldg(&sm->Np), dx = __ldg(&sm->dx), dy = __ldg(&sm->dy);
+      if (!decode_item<kCluster, kTable>(p, it, rank, d)) continue;
+      const TcGroup* gp = SIM_P(d, groups) + d.g;
+      const int Np = SIM_I(d, Np), dx = SIM_I(d, dx), dy = SIM_I(d, dy);
       const int g_nslots = __ldg(&gp->nslots), g_npairs = __ldg(&gp->npairs);
       const int g_rows0 = __ldg(&gp->slot_rows[0]), g_rows1 = __ldg(&gp->slot_rows[1]),
                 g_rows2 = __ldg(&gp->slot_rows[2]);
       const int g_blk0 = __ldg(&gp->slot_block[0]), g_blk1 = __ldg(&gp->slot_block[1]),
                 g_blk2 = __ldg(&gp->slot_block[2]);
-      const Ucoef32* Us = ldg_ptr(&sm->U) + (size_t)d.sl * Np;
-      const float umax_sl = __ldg(ldg_ptr(&sm->umax) + d.sl);
+      const Ucoef32* Us = SIM_P(d, U) + (size_t)d.sl * Np;
+      const float umax_sl = __ldg(SIM_P(d, umax) + d.sl);
       if (umax_sl >= 4.0e6f && tid == 0) atomicExch(p.err, kErrRange);
       const float dlim = 8.0f / fmaxf(umax_sl, 1e-30f);
-      const float* beam = ldg_ptr(&sm->beamT) + (size_t)d.f * __ldg(&sm->PP) * Np;
+      const float* beam = SIM_P(d, beamT) + (size_t)d.f * SIM_I(d, PP) * Np;
       // the slots this CTA fills: all of its group's (no clusters) or the
       // ones it owns (cluster mode)
       const int nfill = kCluster ? nown : g_nslots;
@@ -701,8 +711,8 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
         const int pr = cb >> 1, plane = cb & 1;
         if (pr < g_npairs) {
           const int I = __ldg(&gp->pI[pr]), J = __ldg(&gp->pJ[pr]);
-          float* out = ldg_ptr(&sm->partial) +
-                       (((size_t)d.sl * __ldg(&sm->nchunk) + d.k) * 2 + plane) * (size_t)Np * Np;
+          float* out = SIM_P(d, partial) +
+                       (((size_t)d.sl * SIM_I(d, nchunk) + d.k) * 2 + plane) * (size_t)Np * Np;
           const int a = I * TC_ROWS + q * 32 + lane;
 #pragma unroll 1
           for (int c32 = 0; c32 < 4; ++c32) {
@@ -725,7 +735,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
       ItemInfo d;
       bool ok = true;
       for (long long it = it0; it < p.total_items && ok; it += istep) {
-        if (!decode_item<kCluster>(p, it, rank, d)) continue;
+        if (!decode_item<kCluster, kTable>(p, it, rank, d)) continue;
         for (int j = 0; j < d.nst; ++j, ++gs) {
           const int s = (int)(gs % NS);
           const uint32_t par = (gs / NS) & 1;
@@ -733,7 +743,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
           if (!wait1(rec_empty(s), par ^ 1, abort_flag, p.err)) { ok = false; break; }
           mbar_expect_tx(rec_full(s), TC_REC);
           tma_load_2d(rec_base + (uint32_t)s * TC_REC, &rec_map, rec_full(s), 0,
-                      __ldg(&d.sim->rec_row0) + d.tl * __ldg(&d.sim->rec_stride) + d.s0 +
+                      SIM_I(d, rec_row0) + d.tl * SIM_I(d, rec_stride) + d.s0 +
                           j * TC_KS);
         }
       }
@@ -749,8 +759,8 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
       bool ok = true;
       const uint16_t cmask = kCluster ? (uint16_t)__ldg(&mine->commit_mask) : (uint16_t)1;
       for (long long it = it0; it < p.total_items && ok; it += istep) {
-        if (!decode_item<kCluster>(p, it, rank, d)) continue;
-        const TcGroup* gp = ldg_ptr(&d.sim->groups) + d.g;
+        if (!decode_item<kCluster, kTable>(p, it, rank, d)) continue;
+        const TcGroup* gp = SIM_P(d, groups) + d.g;
         const int n0 = __ldg(&gp->pN[0]), n1 = __ldg(&gp->pN[1]);
         const uint32_t idp0 = idesc_bf16(n0, false), idn0 = idesc_bf16(n0, true);
         const uint32_t idp1 = idesc_bf16(n1, false), idn1 = idesc_bf16(n1, true);
@@ -793,7 +803,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
     ItemInfo d;
     bool ok = true;
     for (long long it = it0; it < p.total_items && ok; it += istep) {
-      if (!decode_item<kCluster>(p, it, rank, d)) continue;
+      if (!decode_item<kCluster, kTable>(p, it, rank, d)) continue;
       for (int j = 0; j < d.nst; ++j, ++gs) {
         const int s = (int)(gs % NS);
         const uint32_t par = (gs / NS) & 1;
@@ -825,6 +835,9 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const TcParams p) {
                  : "memory");
   }
 }
+
+#undef SIM_I
+#undef SIM_P
 
 // ------------------------------------------------------------------- host --
 namespace {
@@ -984,12 +997,14 @@ size_t tc_sim_table_bytes(int nsims) { return sizeof(TcSim) * (size_t)std::max(n
 cudaError_t tc_configure() {
   static bool done = false;
   if (done) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(tc_vis_kernel<false>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_LIMIT);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(tc_vis_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           TC_SMEM_LIMIT);
-  if (e != cudaSuccess) return e;
+  for (const void* k : {reinterpret_cast<const void*>(tc_vis_kernel<false, false>),
+                        reinterpret_cast<const void*>(tc_vis_kernel<false, true>),
+                        reinterpret_cast<const void*>(tc_vis_kernel<true, false>),
+                        reinterpret_cast<const void*>(tc_vis_kernel<true, true>)}) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_LIMIT);
+    if (e != cudaSuccess) return e;
+  }
   done = true;
   return cudaSuccess;
 }
@@ -1045,11 +1060,16 @@ cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, l
     items += (long long)L.nt * L.nf * t.nchunk * (cluster ? 1 : L.ngroups);
   }
   if (items == 0) return cudaSuccess;
-  cudaError_t e = cudaMemcpyAsync(d_table, h_table, sizeof(TcSim) * nsims, cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return e;
+  const bool table = nsims > 1;
+  cudaError_t e = cudaSuccess;
+  if (table) {
+    e = cudaMemcpyAsync(d_table, h_table, sizeof(TcSim) * nsims, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+  }
 
   TcParams p{};
   p.sims = static_cast<const TcSim*>(d_table);
+  p.one = tab[0];
   p.nsims = nsims;
   p.total_items = items;
   p.max_slots = max_slots;
@@ -1063,7 +1083,8 @@ cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, l
   if (e != cudaSuccess) return e;
   if (!cluster) {
     const long long grid = std::min<long long>(num_sms, items);
-    tc_vis_kernel<false><<<(int)grid, TC_THREADS, smem, st>>>(map, p);
+    if (table) tc_vis_kernel<false, true><<<(int)grid, TC_THREADS, smem, st>>>(map, p);
+    else tc_vis_kernel<false, false><<<(int)grid, TC_THREADS, smem, st>>>(map, p);
     return cudaGetLastError();
   }
   // cluster mode: one CTA per group, items are (slice, chunk)
@@ -1082,16 +1103,18 @@ cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, l
   cfg.gridDim = dim3((unsigned)(C * (num_sms / C)));
   // co-resident clusters for this cluster size and shared memory (cached:
   // the query is host-side and stays valid)
-  static int cached_n[TC_MAX_CLUSTER + 1][5] = {};
-  int& nclusters = cached_n[C][p.nstages];
+  static int cached_n[2][TC_MAX_CLUSTER + 1][5] = {};
+  int& nclusters = cached_n[table][C][p.nstages];
   if (nclusters == 0) {
-    e = cudaOccupancyMaxActiveClusters(&nclusters, tc_vis_kernel<true>, &cfg);
+    e = table ? cudaOccupancyMaxActiveClusters(&nclusters, tc_vis_kernel<true, true>, &cfg)
+              : cudaOccupancyMaxActiveClusters(&nclusters, tc_vis_kernel<true, false>, &cfg);
     if (e != cudaSuccess) return e;
   }
   if (nclusters < 1) return cudaErrorInvalidConfiguration;
   const int ncl = (int)std::min<long long>(nclusters, items);
   cfg.gridDim = dim3((unsigned)(C * ncl));
-  e = cudaLaunchKernelEx(&cfg, tc_vis_kernel<true>, map, p);
+  e = table ? cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, true>, map, p)
+            : cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, false>, map, p);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }

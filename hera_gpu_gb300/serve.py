@@ -91,15 +91,20 @@ def make_sky(req: Request, seed: int, lst0: float):
     return req
 
 
+# sources per split-K chunk of a simulation in a batch (hv_batch.cu)
+BATCH_CHUNK = 65536
+
+
 def request_bytes(req: Request, nant: int, P: int) -> int:
     """Device memory one request holds while in flight (inputs, output and its
     share of the batch workspace), for admission against the HBM budget."""
     Np = -(-nant // 128) * 128
     T, F, S = req.ntimes, req.nfreq, max(req.nsrc, 1)
+    nchunk = -(-S // BATCH_CHUNK)  # split-K chunks per slice of the batched kernel
     inputs = 16 * S + 36 * T
     out = 8 * F * T * nant * nant
     work = (4 * F * P * P * Np + 32 * T * F * Np + 32 * T * (S + 32) + 24 * S
-            + 8 * T * F * Np * Np + 8 * 2 ** int(np.ceil(np.log2(max(S, 2048)))))
+            + 8 * T * F * nchunk * Np * Np + 8 * 2 ** int(np.ceil(np.log2(max(S, 2048)))))
     return inputs + out + work
 
 
@@ -115,17 +120,22 @@ class _InFlight:
 
 class _PinnedRing:
     """Page-locked staging of one slot: request inputs and results of the
-    batch in flight on that slot (reallocated, larger, only while idle)."""
+    batch in flight on that slot.  It is reallocated (doubled) only while the
+    slot is idle, and rarely: freeing page-locked memory waits for the whole
+    device, other slots included."""
 
-    def __init__(self, ctx):
+    def __init__(self, ctx, nbytes=64 << 20):
         self.ctx = ctx
-        self.buf = ctx.pinned_empty((1 << 20,), np.uint8)
+        self.buf = ctx.pinned_empty((nbytes,), np.uint8)
         self.off = 0
 
     def reset(self, need):
         if need > self.buf.nbytes:
+            size = self.buf.nbytes
+            while size < need:
+                size *= 2
             self.buf = None
-            self.buf = self.ctx.pinned_empty((int(need * 1.25),), np.uint8)
+            self.buf = self.ctx.pinned_empty((size,), np.uint8)
         self.off = 0
 
     def take(self, shape, dtype):
