@@ -8,9 +8,15 @@
 //
 // Work decomposition
 //   Antennas are cut into blocks of 128 (the MMA M).  The upper triangle of
-//   block pairs (I <= J) is partitioned into groups of at most two pairs that
-//   touch at most three blocks ("slots"); a group's accumulators -- Re V and
-//   Im V for each pair, 128 x 128 FP32 each -- fill the 512 TMEM columns.
+//   block pairs (I <= J) is partitioned into groups of at most two pairs
+//   that share their row block: (I, J) and (I, J + 1), and the pairs that
+//   end a row on the last block, (I, nb - 1), taken transposed as
+//   (nb - 1, I) below the diagonal so that they share the row block nb - 1
+//   (their epilogue writes the conjugate back above it).  A group touches
+//   at most three blocks ("slots") and runs as ONE MMA of N up to 256 per
+//   K-step: the column blocks sit side by side in shared memory, so the row
+//   block's operand is read once for both pairs.  Its accumulators -- Re V
+//   in TMEM columns [0, 256), Im V in [256, 512) -- fill the 512 columns.
 //   A work item is (time, frequency, source chunk, group).  Items are taken
 //   round-robin by a grid of one CTA per SM; each item's partial sum over its
 //   source chunk goes to HBM and a separate kernel reduces the chunks in a
@@ -29,6 +35,8 @@
 //   warp 17       MMA issuer (one thread) and TMEM owner.
 //
 // Operand layout of one stage (32 sources, K = 64 BF16 per antenna row):
+//   the hi tiles of the stage's slots, one after the other, then their lo
+//   tiles (16 KB each: 128 rows x 128 bytes); within a tile
 //   K chunks of 16 bytes: [Re s0-7, Re s8-15, Im s0-7, Im s8-15,
 //                          Re s16-23, Re s24-31, Im s16-23, Im s24-31]
 //   so each MMA K-step (16 elements) holds either the real or the imaginary
@@ -55,7 +63,7 @@ namespace hv {
 constexpr int TC_ROWS = 128;          // antennas per block = MMA M
 constexpr int TC_KS = 32;             // sources per stage
 constexpr int TC_HALF = 16384;        // one operand tile: 128 rows x 128 B
-constexpr int TC_SLOT = 2 * TC_HALF;  // hi + lo tiles of one block
+constexpr int TC_SLOT = 2 * TC_HALF;  // hi + lo tiles of one block (bytes per slot and stage)
 constexpr int TC_REC = TC_KS * 32;    // bytes of source records per stage
 constexpr int TC_GEN_WARPS = 16;
 constexpr int TC_GEN_THREADS = TC_GEN_WARPS * 32;
@@ -76,9 +84,10 @@ struct TcGroup {
   int npairs, nslots;
   int slot_block[3];
   int slot_rows[3];  // valid antenna rows of each slot's block
-  int pa[2], pb[2];  // slots of the row (A) and column (B) operands of each pair
-  int pI[2], pJ[2];  // block indices of each pair
-  int pN[2];         // MMA N of each pair (valid columns of block J, multiple of 16)
+  int sa;            // slot of the row block (A operand); the column blocks (B) are slots 0, 1
+  int n_mma;         // MMA N: 128 + the columns of slot 1 for two pairs, else those of slot 0
+  int pI[2], pJ[2];  // row and column block of each pair; pI > pJ: computed below the diagonal
+  int pN[2];         // valid columns of block pJ, rounded up to 16
   // Cluster mode (one CTA per group, cluster rank = group index): every
   // block is generated by exactly one CTA of the cluster and written into
   // the shared memory of each CTA whose group uses it.
@@ -326,16 +335,19 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint32_t a_lo, uint32_
       : "memory");
 }
 
-// The 24 MMAs of one block pair and one stage (32 sources): for each half
-// of the stage (16 sources) and each split product (hi hi, hi lo, lo hi),
-//   ReV += ReA ReB + ImA ImB,   ImV += ImA ReB - ReA ImB.
-// a, b: descriptor low words of the hi tiles of the pair's row and column
-// blocks (the lo tile follows 16 KB later).  first: the stage opens the item.
-__device__ __forceinline__ void issue_pair(uint32_t d_re, uint32_t a, uint32_t b, uint32_t idp,
-                                           uint32_t idn, bool first) {
-  const uint32_t d_im = d_re + 128;
-  const uint32_t A[2] = {a, a + (TC_HALF >> 4)};
-  const uint32_t B[2] = {b, b + (TC_HALF >> 4)};
+// The 24 MMAs of one group and one stage (32 sources): for each half of
+// the stage (16 sources) and each split product (hi hi, hi lo, lo hi),
+//   ReV += ReA ReB + ImA ImB,   ImV += ImA ReB - ReA ImB,
+// with B the group's column blocks side by side (N up to 256).  a, b:
+// descriptor low words of the hi tiles of the row block and of the first
+// column block; the lo tiles follow lo_step (descriptor units) later.
+// first: the stage opens the item.
+__device__ __forceinline__ void issue_group(uint32_t d_re, uint32_t a, uint32_t b,
+                                            uint32_t lo_step, uint32_t idp, uint32_t idn,
+                                            bool first) {
+  const uint32_t d_im = d_re + 256;
+  const uint32_t A[2] = {a, a + lo_step};
+  const uint32_t B[2] = {b, b + lo_step};
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const uint32_t kre = 4u * h, kim = 4u * h + 2u;  // K-steps of 32 bytes
@@ -553,6 +565,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
   const int NS = p.nstages;
   const uint32_t op_base = smem_u32(smem);
   const uint32_t stage_bytes = (uint32_t)p.max_slots * TC_SLOT;
+  const uint32_t lo_bytes = (uint32_t)p.max_slots * TC_HALF;  // hi tile -> lo tile
   uint8_t* rec_smem = smem + (size_t)NS * stage_bytes;
   const uint32_t rec_base = smem_u32(rec_smem);
   uint64_t* bars = reinterpret_cast<uint64_t*>(rec_smem + (size_t)NS * TC_REC);
@@ -670,8 +683,8 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
           const int h = sg >> 1, sub = sg & 1;
           const uint32_t off_re = rowoff + ((uint32_t)((4 * h + sub) ^ r8) << 4);
           const uint32_t off_im = rowoff + ((uint32_t)((4 * h + 2 + sub) ^ r8) << 4);
-          const uint32_t hi_tile = stage_op + (uint32_t)u_slot[i] * TC_SLOT;
-          const uint32_t lo_tile = hi_tile + TC_HALF;
+          const uint32_t hi_tile = stage_op + (uint32_t)u_slot[i] * TC_HALF;
+          const uint32_t lo_tile = hi_tile + lo_bytes;
           uint4 re_h = make_uint4(0, 0, 0, 0), im_h = re_h, re_l = re_h, im_l = re_h;
           if (u_ok[i]) {
             float rv[8], iv[8];
@@ -707,20 +720,39 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       if (!wait_warp(acc_full, ic & 1, abort_flag, p.err)) break;
       tc_fence_after();
       {
-        const int q = warp & 3, cb = warp >> 2;  // lane quadrant, 128-column block
-        const int pr = cb >> 1, plane = cb & 1;
+        // lane quadrant q, 128-column block cb of TMEM: pair cb & 1, plane
+        // cb >> 1 (Re, Im)
+        const int q = warp & 3, cb = warp >> 2;
+        const int pr = cb & 1, plane = cb >> 1;
         if (pr < g_npairs) {
           const int I = __ldg(&gp->pI[pr]), J = __ldg(&gp->pJ[pr]);
           float* out = SIM_P(d, partial) +
                        (((size_t)d.sl * SIM_I(d, nchunk) + d.k) * 2 + plane) * (size_t)Np * Np;
           const int a = I * TC_ROWS + q * 32 + lane;
+          if (I <= J) {
+            // partial[b][a] = V[a][b], a contiguous across the warp
 #pragma unroll 1
-          for (int c32 = 0; c32 < 4; ++c32) {
-            float v[32];
-            tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cb * 128 + c32 * 32), v);
-            const int b0 = J * TC_ROWS + c32 * 32;
+            for (int c32 = 0; c32 < 4; ++c32) {
+              float v[32];
+              tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cb * 128 + c32 * 32), v);
+              const int b0 = J * TC_ROWS + c32 * 32;
 #pragma unroll
-            for (int c = 0; c < 32; ++c) out[(size_t)(b0 + c) * Np + a] = v[c];
+              for (int c = 0; c < 32; ++c) out[(size_t)(b0 + c) * Np + a] = v[c];
+            }
+          } else {
+            // below the diagonal (a > b): partial[a][b] = V[b][a] = conj V[a][b],
+            // 32 consecutive b per lane
+            const float sg = plane ? -1.f : 1.f;
+#pragma unroll 1
+            for (int c32 = 0; c32 < 4; ++c32) {
+              float v[32];
+              tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cb * 128 + c32 * 32), v);
+              float4* o4 = reinterpret_cast<float4*>(out + (size_t)a * Np + J * TC_ROWS + c32 * 32);
+#pragma unroll
+              for (int c = 0; c < 8; ++c)
+                o4[c] = make_float4(sg * v[4 * c], sg * v[4 * c + 1], sg * v[4 * c + 2],
+                                    sg * v[4 * c + 3]);
+            }
           }
         }
       }
@@ -761,14 +793,11 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       for (long long it = it0; it < p.total_items && ok; it += istep) {
         if (!decode_item<kCluster, kTable>(p, it, rank, d)) continue;
         const TcGroup* gp = SIM_P(d, groups) + d.g;
-        const int n0 = __ldg(&gp->pN[0]), n1 = __ldg(&gp->pN[1]);
-        const uint32_t idp0 = idesc_bf16(n0, false), idn0 = idesc_bf16(n0, true);
-        const uint32_t idp1 = idesc_bf16(n1, false), idn1 = idesc_bf16(n1, true);
-        const uint32_t a0 = desc_lo(op_base + (uint32_t)__ldg(&gp->pa[0]) * TC_SLOT);
-        const uint32_t b0 = desc_lo(op_base + (uint32_t)__ldg(&gp->pb[0]) * TC_SLOT);
-        const uint32_t a1 = desc_lo(op_base + (uint32_t)__ldg(&gp->pa[1]) * TC_SLOT);
-        const uint32_t b1 = desc_lo(op_base + (uint32_t)__ldg(&gp->pb[1]) * TC_SLOT);
-        const bool two = __ldg(&gp->npairs) > 1;
+        const int nm = __ldg(&gp->n_mma);
+        const uint32_t idp = idesc_bf16(nm, false), idn = idesc_bf16(nm, true);
+        const uint32_t a0 = desc_lo(op_base + (uint32_t)__ldg(&gp->sa) * TC_HALF);
+        const uint32_t b0 = desc_lo(op_base);
+        const uint32_t lo_step = lo_bytes >> 4;
         if (!wait1(acc_empty, (ic & 1) ^ 1, abort_flag, p.err)) { ok = false; break; }
         tc_fence_after();
         for (int j = 0; j < d.nst; ++j, ++gs) {
@@ -780,8 +809,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
           if (recv_bytes) mbar_expect_tx(smem_full(s), recv_bytes);
           tc_fence_after();
           const uint32_t so = ((uint32_t)s * stage_bytes) >> 4;
-          issue_pair(tmem, a0 + so, b0 + so, idp0, idn0, j == 0);
-          if (two) issue_pair(tmem + 256, a1 + so, b1 + so, idp1, idn1, j == 0);
+          issue_group(tmem, a0 + so, b0 + so, lo_step, idp, idn, j == 0);
           // the stage's slots may be refilled -- here and, in cluster mode,
           // by the CTAs that wrote them -- once these MMAs have read them
           if (kCluster && cmask != (uint16_t)(1u << rank)) mma_commit_multicast(smem_empty(s), cmask);
@@ -810,12 +838,14 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
         if (!wait1(gen_done(s), par, abort_flag, p.err)) { ok = false; break; }
         const uint32_t stage_op = op_base + (uint32_t)s * stage_bytes;
         for (int k = 0; k < nown; ++k) {
-          const uint32_t src = stage_op + (uint32_t)__ldg(&mine->own_slot[k]) * TC_SLOT;
+          const uint32_t src = stage_op + (uint32_t)__ldg(&mine->own_slot[k]) * TC_HALF;
           const int nd = __ldg(&mine->ndst[k]);
           for (int q = 0; q < nd; ++q) {
             const uint32_t rr = (uint32_t)__ldg(&mine->dst_rank[k][q]);
-            const uint32_t dst = stage_op + (uint32_t)__ldg(&mine->dst_slot[k][q]) * TC_SLOT;
-            bulk_push(map_to_rank(dst, rr), src, TC_SLOT, map_to_rank(smem_full(s), rr));
+            const uint32_t dst = stage_op + (uint32_t)__ldg(&mine->dst_slot[k][q]) * TC_HALF;
+            const uint32_t bar = map_to_rank(smem_full(s), rr);
+            bulk_push(map_to_rank(dst, rr), src, TC_HALF, bar);                        // hi
+            bulk_push(map_to_rank(dst + lo_bytes, rr), src + lo_bytes, TC_HALF, bar);  // lo
           }
         }
       }
@@ -846,31 +876,22 @@ std::vector<TcGroup> make_groups(int nant) {
   const int nb = ceil_div(nant, TC_ROWS);
   auto rows_of = [&](int blk) { return std::min(TC_ROWS, nant - blk * TC_ROWS); };
   auto ncols = [&](int blk) { return ((rows_of(blk) + 15) / 16) * 16; };
+  // (row block, column block) pairs of each group; the column blocks of a
+  // group are different and only the last may be partly valid
   std::vector<std::vector<std::pair<int, int>>> raw;
-  std::vector<std::pair<int, int>> singles;
+  std::vector<int> singles;  // rows whose last pair (I, nb - 1) is left over
   for (int I = 0; I < nb; ++I) {
     int J = I;
     for (; J + 1 < nb; J += 2) raw.push_back({{I, J}, {I, J + 1}});
-    if (J < nb) singles.push_back({I, J});
+    if (J < nb) singles.push_back(I);
   }
-  // merge single pairs when the two touch at most three blocks
-  std::vector<bool> used(singles.size(), false);
-  for (size_t i = 0; i < singles.size(); ++i) {
-    if (used[i]) continue;
-    used[i] = true;
-    bool merged = false;
-    for (size_t k = i + 1; k < singles.size() && !merged; ++k) {
-      if (used[k]) continue;
-      int blocks[4] = {singles[i].first, singles[i].second, singles[k].first, singles[k].second};
-      std::sort(blocks, blocks + 4);
-      const int distinct = (int)(std::unique(blocks, blocks + 4) - blocks);
-      if (distinct <= 3) {
-        raw.push_back({singles[k], singles[i]});
-        used[k] = true;
-        merged = true;
-      }
-    }
-    if (!merged) raw.push_back({singles[i]});
+  // the left-over pairs all end on block nb - 1: taken as (nb - 1, I) they
+  // share the row block, two per group (ascending I, so the diagonal pair
+  // (nb - 1, nb - 1), whose block may be partial, comes last)
+  for (size_t k = 0; k < singles.size(); k += 2) {
+    std::vector<std::pair<int, int>> g{{nb - 1, singles[k]}};
+    if (k + 1 < singles.size()) g.push_back({nb - 1, singles[k + 1]});
+    raw.push_back(g);
   }
   std::vector<TcGroup> out;
   for (auto& prs : raw) {
@@ -884,13 +905,15 @@ std::vector<TcGroup> make_groups(int nant) {
       g.slot_rows[g.nslots] = rows_of(blk);
       return g.nslots++;
     };
+    // column blocks first (slots 0 and 1, side by side), then the row block
     for (int q = 0; q < g.npairs; ++q) {
       g.pI[q] = prs[q].first;
       g.pJ[q] = prs[q].second;
-      g.pa[q] = slot_of(prs[q].first);
-      g.pb[q] = slot_of(prs[q].second);
       g.pN[q] = ncols(prs[q].second);
+      slot_of(prs[q].second);
     }
+    g.sa = slot_of(prs[0].first);
+    g.n_mma = g.npairs == 2 ? TC_ROWS + g.pN[1] : g.pN[0];
     out.push_back(g);
   }
   return out;
