@@ -157,13 +157,17 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
                : "memory");
 }
+// try_wait with a suspend-time hint: a waiting thread sleeps in hardware
+// until the phase completes or the hint (ns) elapses, instead of polling
+// the barrier through the shared-memory pipe.
+constexpr uint32_t kSuspendHintNs = 20000;
 __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
       " selp.u32 %0, 1, 0, p;\n}\n"
       : "=r"(ok)
-      : "r"(bar), "r"(parity)
+      : "r"(bar), "r"(parity), "r"(kSuspendHintNs)
       : "memory");
   return ok != 0;
 }
@@ -250,10 +254,10 @@ __device__ __forceinline__ void mbar_arrive_cluster(uint32_t remote_bar) {
 __device__ __forceinline__ bool mbar_try_cluster(uint32_t bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2, %3;\n"
       " selp.u32 %0, 1, 0, p;\n}\n"
       : "=r"(ok)
-      : "r"(bar), "r"(parity)
+      : "r"(bar), "r"(parity), "r"(kSuspendHintNs)
       : "memory");
   return ok != 0;
 }
@@ -666,6 +670,9 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
         u_ok[i] = i < nfill && row < srows;
         u_a[i] = sblk * TC_ROWS + row;
       }
+      // the phase coefficients of the first unit's antenna, fixed for the item
+      Ucoef32 uc0 = {};
+      if (u_ok[0]) uc0 = Us[u_a[0]];
       const int row = tid & (TC_ROWS - 1);
       const int r8 = row & 7;
       const uint32_t rowoff = (uint32_t)(row >> 3) * 1024u + (uint32_t)r8 * 128u;
@@ -688,7 +695,8 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
           uint4 re_h = make_uint4(0, 0, 0, 0), im_h = re_h, re_l = re_h, im_l = re_h;
           if (u_ok[i]) {
             float rv[8], iv[8];
-            gen_unit(recs + sg * 8, Us[u_a[i]], beam + u_a[i], Np, dx, dy, dlim, rv, iv);
+            gen_unit(recs + sg * 8, i == 0 ? uc0 : Us[u_a[i]], beam + u_a[i], Np, dx, dy, dlim,
+                     rv, iv);
             split_pack(rv, re_h, re_l);
             split_pack(iv, im_h, im_l);
           }
@@ -698,8 +706,11 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
           sts128(lo_tile + off_im, im_l);
         };
         if (kCluster) {
-#pragma unroll 1
-          for (int i = 0; i < nfill; ++i) unit(i);
+          // static unit indices keep the unit tables in registers (a CTA that
+          // generates owns at least one slot)
+          unit(0);
+          if (nfill > 1) unit(1);
+          if (nfill > 2) unit(2);
         } else {
 #pragma unroll
           for (int i = 0; i < 3; ++i)
