@@ -55,6 +55,7 @@ SIGNATURES = {
     "hv_sync": (_c_int, [_c_void_p]),
     "hv_set_profiling": (_c_int, [_c_void_p, _c_int]),
     "hv_profile_read": (_c_int, [_c_void_p, ctypes.POINTER(_c_double), ctypes.POINTER(ctypes.c_uint64)]),
+    "hv_set_wait_limit": (_c_int, [_c_void_p, ctypes.c_uint64, _c_int]),
     "hv_vis_gpu_noalloc": (_c_int, [_PTR, _c_int, _c_double, _PTR, _c_int, _PTR, _PTR, _c_int,
                                     _PTR, _c_int, _PTR, _c_void_p, ctypes.c_char_p, _c_size_t]),
     "hv_batch_create": (_c_int, [_c_void_p, ctypes.POINTER(HvSim), _c_int, ctypes.c_uint,
@@ -206,6 +207,12 @@ class Context:
 
     def set_profiling(self, enable: bool):
         self.check(self.lib.hv_set_profiling(self.h, 1 if enable else 0))
+
+    def set_wait_limit(self, wait_s: float = 0.0, stall: bool = False):
+        """Limit of each device-side wait of the fused kernel (0: 2 s); with
+        ``stall`` the next fused launches are made to time out (fault
+        injection for tests of failure detection)."""
+        self.check(self.lib.hv_set_wait_limit(self.h, int(wait_s * 1e9), 1 if stall else 0))
 
     def profile_read(self):
         """(milliseconds, launches) of the visibility-product kernels since

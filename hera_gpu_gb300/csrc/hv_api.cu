@@ -49,6 +49,10 @@ struct hv_context {
   int* d_err = nullptr;  // device-side error flag (bounded waits)
   // profiling of the visibility-product kernels
   bool profiling = false;
+  // device-side wait limit of the fused kernel (0: its default) and fault
+  // injection (hv_set_wait_limit)
+  uint64_t wait_ns = 0;
+  int stall = 0;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
   // staging of host-API inputs / outputs
   DevBuf in_antpos, in_eq2tops, in_crd, in_I, in_bm, out_vis;
@@ -280,7 +284,7 @@ int run_device(hv_context* ctx, int method, const R* antpos, int nant, const dou
         if (nsrc > 0)
           HV_LAUNCH_TIMED(launch_tc_batch(&L, 1, ctx->rec.p, (long long)nt * rec_stride,
                                           ctx->tctable.p, ctx->tctable_h.p, ctx->d_err,
-                                          ctx->num_sms, st),
+                                          ctx->num_sms, st, ctx->wait_ns, ctx->stall),
                           st);
         HV_LAUNCH(1, launch_reduce<float>(static_cast<float*>(ctx->partial.p), slice_floats,
                                           counts + t0, nt, nfreq, t0, ntimes, chunk, Np, nant,
@@ -382,6 +386,8 @@ void hv_context_record_kernel(hv_context* ctx, cudaEvent_t e0, cudaEvent_t e1) {
 }
 
 bool hv_context_profiling(hv_context* ctx) { return ctx->profiling; }
+uint64_t hv_context_wait_ns(hv_context* ctx) { return ctx->wait_ns; }
+int hv_context_stall(hv_context* ctx) { return ctx->stall; }
 
 extern "C" {
 
@@ -525,6 +531,13 @@ int hv_vis_gpu(hv_context* ctx, int precision, int method, const void* antpos, i
 int hv_set_profiling(hv_context* ctx, int enable) {
   if (!ctx) return HV_ERR_ARG;
   ctx->profiling = enable != 0;
+  return HV_OK;
+}
+
+int hv_set_wait_limit(hv_context* ctx, uint64_t wait_ns, int stall) {
+  if (!ctx) return HV_ERR_ARG;
+  ctx->wait_ns = wait_ns;
+  ctx->stall = stall != 0;
   return HV_OK;
 }
 

@@ -280,7 +280,7 @@ int enqueue(hv_batch* b, cudaStream_t st, int timed_class = -1) {
       }
       HB_CK(launch_tc_batch(d.data(), (int)d.size(), b->rec, b->rec_rows,
                             static_cast<char*>(b->table) + toff, H + b->h_table + toff, b->d_err,
-                            b->num_sms, st));
+                            b->num_sms, st, hv_context_wait_ns(b->ctx), hv_context_stall(b->ctx)));
       if (prof) {
         HB_CK(cudaEventRecord(e1, st));
         hv_context_record_kernel(b->ctx, e0, e1);

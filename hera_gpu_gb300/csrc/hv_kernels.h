@@ -107,10 +107,12 @@ cudaError_t tc_configure();
 // rows (rewritten by launch_tc_relative) of every simulation, rec_rows in
 // all.  d_table / h_table: device and host (kept alive until the copy ran)
 // buffers of tc_sim_table_bytes(nsims).  Cluster mode is used when every
-// simulation has the same clusterable group layout.
+// simulation has the same clusterable group layout.  wait_ns: limit of
+// each device-side wait (0: 2 s); stall: fault injection (the first record
+// copy is never issued, so the launch ends with a timeout status).
 cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, long long rec_rows,
                             void* d_table, void* h_table, int* err, int num_sms,
-                            cudaStream_t st);
+                            cudaStream_t st, unsigned long long wait_ns = 0, int stall = 0);
 size_t tc_partial_floats(int Np, int nsrc, int nslices, int chunk);
 int tc_chunk_sources(int nsrc, int nslices, int ngroups, int num_sms);
 size_t tc_group_table_bytes(int nant);
@@ -133,3 +135,6 @@ void hv_context_host_give(hv_context* ctx, void* p, size_t cap);
 // Profiling: the context owns and times the pair of recorded events.
 bool hv_context_profiling(hv_context* ctx);
 void hv_context_record_kernel(hv_context* ctx, cudaEvent_t e0, cudaEvent_t e1);
+// Wait limit and fault injection of the fused kernel (hv_set_wait_limit).
+uint64_t hv_context_wait_ns(hv_context* ctx);
+int hv_context_stall(hv_context* ctx);

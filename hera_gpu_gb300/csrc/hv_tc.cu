@@ -73,7 +73,7 @@ constexpr int TC_PUSH_WARP = TC_GEN_WARPS + 2;  // cluster mode: pushes tiles to
 constexpr int TC_THREADS = TC_GEN_THREADS + 96;
 constexpr int TC_TMEM_COLS = 512;
 constexpr int TC_SMEM_LIMIT = 227 * 1024;
-constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // 2 s per wait
+constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // default limit of one wait: 2 s
 
 constexpr int kErrTimeout = 1;
 constexpr int kErrRange = 2;    // |U| beyond the exact range of rint_magic
@@ -130,6 +130,8 @@ struct TcParams {
   long long total_items;
   int nstages, max_slots;
   int* err;
+  unsigned long long wait_ns;  // limit of one wait
+  int stall;                   // fault injection: the first record copy is never issued
 };
 
 // Read-only load of a pointer-valued field.
@@ -178,13 +180,13 @@ __device__ __forceinline__ bool mbar_try_cluster(uint32_t bar, uint32_t parity);
 // that threads of other CTAs arrive on).
 template <bool kCl = false>
 __device__ __forceinline__ bool wait1(uint32_t bar, uint32_t parity, volatile int* abort_flag,
-                                      int* gerr) {
+                                      int* gerr, unsigned long long limit_ns) {
   const unsigned long long t0 = global_ns();
   for (uint32_t i = 0;; ++i) {
     if (kCl ? mbar_try_cluster(bar, parity) : mbar_try(bar, parity)) return true;
     if ((i & 63) == 63) {
       if (*abort_flag) return false;
-      if (global_ns() - t0 > TC_WAIT_NS) {
+      if (global_ns() - t0 > limit_ns) {
         *abort_flag = 1;
         atomicExch(gerr, kErrTimeout);
         return false;
@@ -196,7 +198,7 @@ __device__ __forceinline__ bool wait1(uint32_t bar, uint32_t parity, volatile in
 // Whole-warp bounded wait; the outcome is uniform across the warp.
 template <bool kCl = false>
 __device__ __forceinline__ bool wait_warp(uint32_t bar, uint32_t parity, volatile int* abort_flag,
-                                          int* gerr) {
+                                          int* gerr, unsigned long long limit_ns) {
   const unsigned long long t0 = global_ns();
   for (uint32_t i = 0;; ++i) {
     const bool done = kCl ? mbar_try_cluster(bar, parity) : mbar_try(bar, parity);
@@ -207,7 +209,7 @@ __device__ __forceinline__ bool wait_warp(uint32_t bar, uint32_t parity, volatil
       if ((threadIdx.x & 31) == 0) {
         if (*abort_flag) {
           give_up = 1;
-        } else if (global_ns() - t0 > TC_WAIT_NS) {
+        } else if (global_ns() - t0 > limit_ns) {
           *abort_flag = 1;
           atomicExch(gerr, kErrTimeout);
           give_up = 1;
@@ -220,11 +222,12 @@ __device__ __forceinline__ bool wait_warp(uint32_t bar, uint32_t parity, volatil
 
 // Bounded wait used while shutting down: ignores the abort flag so that
 // copies and MMAs already in flight still land before TMEM is released.
-__device__ __forceinline__ void wait_drain(uint32_t bar, uint32_t parity, int* gerr) {
+__device__ __forceinline__ void wait_drain(uint32_t bar, uint32_t parity, int* gerr,
+                                           unsigned long long limit_ns) {
   const unsigned long long t0 = global_ns();
   for (uint32_t i = 0;; ++i) {
     if (mbar_try(bar, parity)) return;
-    if ((i & 63) == 63 && global_ns() - t0 > TC_WAIT_NS) {
+    if ((i & 63) == 63 && global_ns() - t0 > limit_ns) {
       atomicExch(gerr, kErrTimeout);
       return;
     }
@@ -681,8 +684,8 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       for (int j = 0; j < d.nst && ok && generates; ++j, ++gs) {
         const int s = (int)(gs % NS);
         const uint32_t par = (gs / NS) & 1;
-        if (!wait_warp(rec_full(s), par, abort_flag, p.err)) { ok = false; break; }
-        if (!wait_warp<kCluster>(smem_empty(s), par ^ 1, abort_flag, p.err)) { ok = false; break; }
+        if (!wait_warp(rec_full(s), par, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
+        if (!wait_warp<kCluster>(smem_empty(s), par ^ 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
         const SrcRec32* recs = reinterpret_cast<const SrcRec32*>(rec_smem + (size_t)s * TC_REC);
         const uint32_t stage_op = op_base + (uint32_t)s * stage_bytes;
         auto unit = [&](int i) {
@@ -728,7 +731,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       }
       if (!ok) break;
       // ------------------------------------------------------- epilogue --
-      if (!wait_warp(acc_full, ic & 1, abort_flag, p.err)) break;
+      if (!wait_warp(acc_full, ic & 1, abort_flag, p.err, p.wait_ns)) break;
       tc_fence_after();
       {
         // lane quadrant q, 128-column block cb of TMEM: pair cb & 1, plane
@@ -783,7 +786,9 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
           const int s = (int)(gs % NS);
           const uint32_t par = (gs / NS) & 1;
           // this CTA's generators have finished reading the previous round
-          if (!wait1(rec_empty(s), par ^ 1, abort_flag, p.err)) { ok = false; break; }
+          if (!wait1(rec_empty(s), par ^ 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
+          // fault injection: stage 0 never fills, so its consumers time out
+          if (p.stall && gs == 0) continue;
           mbar_expect_tx(rec_full(s), TC_REC);
           tma_load_2d(rec_base + (uint32_t)s * TC_REC, &rec_map, rec_full(s), 0,
                       SIM_I(d, rec_row0) + d.tl * SIM_I(d, rec_stride) + d.s0 +
@@ -792,7 +797,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       }
       // let the copies still in flight land before the CTA can exit
       const uint32_t first = gs > (uint32_t)NS ? gs - NS : 0;
-      for (uint32_t g = first; g < gs; ++g) wait_drain(rec_full((int)(g % NS)), (g / NS) & 1, p.err);
+      for (uint32_t g = first; g < gs; ++g) wait_drain(rec_full((int)(g % NS)), (g / NS) & 1, p.err, p.wait_ns);
     }
   } else if (warp == TC_MMA_WARP) {
     // ------------------------------------------------------- MMA issuer --
@@ -809,12 +814,12 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
         const uint32_t a0 = desc_lo(op_base + (uint32_t)__ldg(&gp->sa) * TC_HALF);
         const uint32_t b0 = desc_lo(op_base);
         const uint32_t lo_step = lo_bytes >> 4;
-        if (!wait1(acc_empty, (ic & 1) ^ 1, abort_flag, p.err)) { ok = false; break; }
+        if (!wait1(acc_empty, (ic & 1) ^ 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
         tc_fence_after();
         for (int j = 0; j < d.nst; ++j, ++gs) {
           const int s = (int)(gs % NS);
           const uint32_t par = (gs / NS) & 1;
-          if (!wait1(smem_full(s), par, abort_flag, p.err)) { ok = false; break; }
+          if (!wait1(smem_full(s), par, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
           // arm the next round of this stage for the peers' pushes (they can
           // only come after this round's MMAs release the slot)
           if (recv_bytes) mbar_expect_tx(smem_full(s), recv_bytes);
@@ -832,7 +837,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       }
       // every MMA issued by this thread completes before TMEM is released
       mma_commit(drain);
-      wait_drain(drain, 0, p.err);
+      wait_drain(drain, 0, p.err, p.wait_ns);
     }
   }
 
@@ -846,7 +851,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       for (int j = 0; j < d.nst; ++j, ++gs) {
         const int s = (int)(gs % NS);
         const uint32_t par = (gs / NS) & 1;
-        if (!wait1(gen_done(s), par, abort_flag, p.err)) { ok = false; break; }
+        if (!wait1(gen_done(s), par, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
         const uint32_t stage_op = op_base + (uint32_t)s * stage_bytes;
         for (int k = 0; k < nown; ++k) {
           const uint32_t src = stage_op + (uint32_t)__ldg(&mine->own_slot[k]) * TC_HALF;
@@ -1045,7 +1050,7 @@ cudaError_t tc_configure() {
 
 cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, long long rec_rows,
                             void* d_table, void* h_table, int* err, int num_sms,
-                            cudaStream_t st) {
+                            cudaStream_t st, unsigned long long wait_ns, int stall) {
   if (nsims <= 0 || rec_rows <= 0) return cudaSuccess;
   auto encode = encode_fn();
   if (!encode) return cudaErrorNotSupported;
@@ -1108,6 +1113,8 @@ cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, l
   p.total_items = items;
   p.max_slots = max_slots;
   p.err = err;
+  p.wait_ns = wait_ns ? wait_ns : TC_WAIT_NS;
+  p.stall = stall;
   const int per_stage = p.max_slots * TC_SLOT + TC_REC;
   const int fixed = 1024 /*alignment*/ + 512 /*barriers, holder*/;
   p.nstages = std::min(4, (TC_SMEM_LIMIT - fixed) / per_stage);

@@ -16,6 +16,12 @@ a simulation service sees a stream of requests of uneven size.  This loop:
 * records per request the latency from arrival to the result being in host
   memory, and reports p50 / p99 latency and the visibility throughput.
 
+Failures stay with the requests they hit: a request that can never fit the
+HBM budget is rejected on arrival, a cancelled request is dropped before it
+is admitted, and a batch whose launch or device-side waits fail (a CUDA
+error, a bounded wait that ran out) marks its own requests failed while the
+loop goes on serving the others.
+
 A request's result does not depend on which other requests share its batch:
 every simulation of a batch keeps its own work items, split-K chunks and
 reduction order.
@@ -71,6 +77,16 @@ class Request:
     t_start: float = 0.0
     t_done: float = 0.0
     nant: int = 0
+    error: str = None               # why the request was not served
+    cancelled: bool = False
+
+    def cancel(self):
+        """Drop the request if it has not been admitted yet."""
+        self.cancelled = True
+
+    @property
+    def ok(self):
+        return self.result is not None and self.error is None
 
     @property
     def latency(self):
@@ -147,16 +163,23 @@ class _PinnedRing:
 
 
 class Server:
-    """Continuous-batching loop over ``slots`` device streams."""
+    """Continuous-batching loop over ``slots`` device streams (one context
+    each).  ``batch_factory(ctx, sims)`` builds a batch (default
+    :class:`_native.Batch`)."""
 
-    def __init__(self, sets, contexts, hbm_budget=150e9, max_batch=64):
+    def __init__(self, sets, contexts, hbm_budget=150e9, max_batch=64, batch_factory=None):
         self.sets = sets
         self.ctxs = contexts
         self.budget = float(hbm_budget)
         self.max_batch = int(max_batch)
+        self.batch_factory = batch_factory or _native.Batch
         self.rings = [_PinnedRing(c) for c in contexts]
+        self.max_held = 0.0  # largest device memory admitted at once (bytes)
 
     def _launch(self, slot, reqs):
+        """Copy the requests' inputs in, launch their batch and queue the
+        result copies, all on the slot's stream.  Returns the in-flight record,
+        or None when the launch failed (the requests then carry the error)."""
         ctx = self.ctxs[slot]
         ring = self.rings[slot]
         need = 0
@@ -166,31 +189,41 @@ class Server:
             need += 8 * r.nfreq * r.ntimes * rs.nant * rs.nant + 256
         ring.reset(need)
         bufs, outs, sims = [], [], []
-        for r in reqs:
-            rs = self.sets[r.set_id]
-            r.nant = rs.nant
-            d = {}
-            for name in ("crd_eq", "I_sky", "eq2tops"):
-                a = getattr(r, name)
-                h = ring.take(a.shape, a.dtype)
-                h[...] = a
-                d[name] = ctx.device_alloc(a.nbytes)
-                ctx.h2d(d[name], h)
-                bufs.append(d[name])
-            out = ring.take((r.nfreq, r.ntimes, rs.nant, rs.nant), np.complex64)
-            outs.append(out)
-            d["out"] = ctx.device_alloc(out.nbytes)
-            bufs.append(d["out"])
-            sims.append(dict(antpos=rs.d_antpos, eq2tops=d["eq2tops"], crd_eq=d["crd_eq"],
-                             I_sky=d["I_sky"], bm_cubes=rs.d_bm, freqs=rs.freqs[:r.nfreq],
-                             vis_out=d["out"], nant=rs.nant, ntimes=r.ntimes, nsrc=r.nsrc,
-                             beam_px=rs.P))
-        batch = _native.Batch(ctx, sims)
-        batch.launch()
-        for out, s in zip(outs, sims):
-            ctx.d2h(out, s["vis_out"])
         nbytes = sum(request_bytes(r, self.sets[r.set_id].nant, self.sets[r.set_id].P)
                      for r in reqs)
+        batch = None
+        try:
+            for r in reqs:
+                rs = self.sets[r.set_id]
+                r.nant = rs.nant
+                d = {}
+                for name in ("crd_eq", "I_sky", "eq2tops"):
+                    a = getattr(r, name)
+                    h = ring.take(a.shape, a.dtype)
+                    h[...] = a
+                    d[name] = ctx.device_alloc(a.nbytes)
+                    bufs.append(d[name])
+                    ctx.h2d(d[name], h)
+                out = ring.take((r.nfreq, r.ntimes, rs.nant, rs.nant), np.complex64)
+                outs.append(out)
+                d["out"] = ctx.device_alloc(out.nbytes)
+                bufs.append(d["out"])
+                sims.append(dict(antpos=rs.d_antpos, eq2tops=d["eq2tops"], crd_eq=d["crd_eq"],
+                                 I_sky=d["I_sky"], bm_cubes=rs.d_bm, freqs=rs.freqs[:r.nfreq],
+                                 vis_out=d["out"], nant=rs.nant, ntimes=r.ntimes, nsrc=r.nsrc,
+                                 beam_px=rs.P))
+            batch = self.batch_factory(ctx, sims)
+            batch.launch()
+        except _native.HeraVisError as e:
+            if batch is not None:
+                batch.close()
+            for b in bufs:
+                ctx.device_free(b)
+            for r in reqs:
+                r.error = f"launch failed: {e}"
+            return None
+        for out, s in zip(outs, sims):
+            ctx.d2h(out, s["vis_out"])
         return _InFlight(slot, batch, reqs, bufs, outs, nbytes)
 
     def run(self, requests, clock=time.perf_counter, poll_s=2e-4):
@@ -211,12 +244,19 @@ class Server:
             for slot in list(inflight):
                 f = inflight[slot]
                 if self.ctxs[slot].idle():
+                    try:
+                        f.batch.sync()  # device-side errors of the batch (timeouts)
+                        err = None
+                    except _native.HeraVisError as e:
+                        err = f"batch failed: {e}"
                     for r, out in zip(f.reqs, f.outs):
-                        r.result = out.copy()
+                        if err is None:
+                            r.result = out.copy()
+                        else:
+                            r.error = err
                     t = clock() - t0
                     for r in f.reqs:
                         r.t_done = t
-                    f.batch.sync()
                     f.batch.close()
                     for b in f.buffers:
                         self.ctxs[slot].device_free(b)
@@ -231,9 +271,16 @@ class Server:
                     r = pending[0]
                     rs = self.sets[r.set_id]
                     need = request_bytes(r, rs.nant, rs.P)
-                    if take and held + nb + need > self.budget:
-                        break
-                    if not take and inflight and held + need > self.budget:
+                    if r.cancelled or need > self.budget:
+                        # never admitted: cancelled, or larger than the budget
+                        pending.popleft()
+                        r.error = "cancelled" if r.cancelled else (
+                            f"needs {need / 1e9:.2f} GB, above the HBM budget of "
+                            f"{self.budget / 1e9:.2f} GB")
+                        r.t_done = clock() - t0
+                        progressed = True
+                        continue
+                    if held + nb + need > self.budget:
                         break  # wait for memory to free up
                     take.append(pending.popleft())
                     nb += need
@@ -242,9 +289,15 @@ class Server:
                 t = clock() - t0
                 for r in take:
                     r.t_start = t
-                inflight[slot] = self._launch(slot, take)
-                held += inflight[slot].nbytes
+                f = self._launch(slot, take)
                 progressed = True
+                if f is None:  # the launch failed: its requests carry the error
+                    for r in take:
+                        r.t_done = clock() - t0
+                    continue
+                inflight[slot] = f
+                held += f.nbytes
+                self.max_held = max(self.max_held, held)
             if not progressed:
                 nxt = requests[i].arrival - (clock() - t0) if i < len(requests) else poll_s
                 time.sleep(max(0.0, min(poll_s, nxt)))
@@ -252,9 +305,14 @@ class Server:
 
 
 def summarize(requests, wall_s):
-    lat = np.array([r.latency for r in requests])
-    vis = sum(r.visibilities for r in requests)
-    return {"requests": len(requests), "p50_ms": float(np.percentile(lat, 50) * 1e3),
+    """Latency percentiles and throughput over the served requests."""
+    done = [r for r in requests if r.ok]
+    lat = np.array([r.latency for r in done]) if done else np.zeros(1)
+    vis = sum(r.visibilities for r in done)
+    return {"requests": len(requests), "served": len(done),
+            "failed": sum(1 for r in requests if r.error and not r.cancelled),
+            "cancelled": sum(1 for r in requests if r.cancelled),
+            "p50_ms": float(np.percentile(lat, 50) * 1e3),
             "p99_ms": float(np.percentile(lat, 99) * 1e3),
             "mean_ms": float(lat.mean() * 1e3), "vis_per_s": vis / wall_s, "wall_s": wall_s}
 

@@ -117,6 +117,14 @@ int hv_sync(hv_context* ctx);
 int hv_set_profiling(hv_context* ctx, int enable);
 int hv_profile_read(hv_context* ctx, double* ms, uint64_t* launches);
 
+/* Limit of each device-side wait of the fused kernel in this context
+ * (wait_ns = 0: 2 s), and fault injection for tests of failure detection:
+ * with stall set, the next fused launches never issue their first source
+ * copy, so their consumers' bounded waits run out and the call returns
+ * HV_ERR_TIMEOUT with the context still usable.  No counterpart in the
+ * reference (it has no device-side waits, hera_gpu/vis.py:144-250). */
+int hv_set_wait_limit(hv_context* ctx, uint64_t wait_ns, int stall);
+
 /* ---- batched form -------------------------------------------------------
  * Many independent simulations (precision 1, fused tensor-core form) planned
  * and run together: the reference's per-call vis_gpu (vis.py:144-262) applied
