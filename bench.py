@@ -59,6 +59,10 @@ def parse_args():
     ap.add_argument("--serve-requests", type=int, default=400,
                     help="requests of the serving leg (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-rate-low", type=float, default=100.0,
+                    help="a second serving run at this rate (0 = skip)")
+    ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--serve-max-batch", type=int, default=2)
     return ap.parse_args()
 
 
@@ -479,33 +483,58 @@ def run_serve(args, device, pool):
     """The serving configuration: Poisson arrivals at --serve-rate of requests
     from the batched-form size distribution plus 5 % large requests (350
     antennas, 1M sources, 60 LSTs), 8 resident beam/layout sets, HBM budget
-    150 GB, 4 slots.  Latency = arrival to result in host memory."""
+    150 GB, --serve-slots slots of at most --serve-max-batch requests.
+    Latency = arrival to result in host memory.  A second run at
+    --serve-rate-low shows the latency below saturation."""
     import numpy as np
     from hera_gpu_gb300 import _native, serve
+    ctxs = [_native.Context(device) for _ in range(args.serve_slots)]
     specs, reqs = serve.workload(args.serve_requests, rate_hz=args.serve_rate, seed=7)
-    ctxs = [_native.Context(device) for _ in range(4)]
     sets = serve.build_sets(ctxs[0], specs, nfreq=16)
-    # warm the plan/launch path once (first-use costs are not steady state)
+    srv = serve.Server(sets, ctxs, hbm_budget=150e9, max_batch=args.serve_max_batch)
+    # page-locked staging sized up front, and the plan/launch path warmed
+    # once (first-use costs are not steady state)
+    srv.reserve(reqs)
     warm = serve.workload(4, rate_hz=1e4, large_frac=0.0, seed=99)[1]
-    for r in warm:
-        r.set_id = r.set_id % len(sets)
-    srv = serve.Server(sets, ctxs, hbm_budget=150e9, max_batch=32)
     srv.run(warm)
-    done = srv.run(reqs)
-    wall = max(r.t_done for r in done)
-    out = serve.summarize(done, wall)
+
+    # the oracle sample: 1 % of the small requests, one (time, channel) slice
+    # each, kept by the result consumer (the other results are delivered and
+    # dropped, as a service hands them on)
+    rng = np.random.default_rng(3)
+    small_ids = [r.rid for r in reqs if r.nsrc < 100_000]
+    sample_ids = set(rng.choice(small_ids, size=max(1, len(reqs) // 100), replace=False).tolist())
+    kept = {}
+
+    def consume(r, view):
+        if r.rid in sample_ids:
+            kept[r.rid] = view[0, 0].copy()
+
+    def one_run(rs, keep):
+        done = srv.run(rs, on_result=consume if keep else (lambda r, v: None))
+        out = serve.summarize(done, max(r.t_done for r in done))
+        out["offered_req_per_s"] = len(rs) / max(r.arrival for r in rs)
+        return done, out
+
+    done, out = one_run(reqs, True)
     out.update({"rate_hz": args.serve_rate, "large_frac": 0.05, "slots": len(ctxs),
-                "resident_sets": len(sets), "hbm_budget_gb": 150,
-                "latency": "arrival to result in host memory"})
+                "max_batch": args.serve_max_batch, "resident_sets": len(sets),
+                "hbm_budget_gb": 150,
+                "latency": "arrival to result in host memory (page-locked staging, handed to a "
+                           "consumer callback)"})
+    if args.serve_rate_low > 0:
+        _, reqs_low = serve.workload(args.serve_requests, rate_hz=args.serve_rate_low, seed=7)
+        _, low = one_run(reqs_low, False)
+        out["at_lower_rate"] = {k: low[k] for k in ("offered_req_per_s", "p50_ms", "p99_ms",
+                                                    "mean_ms", "vis_per_s", "wall_s", "served")}
+        out["at_lower_rate"]["rate_hz"] = args.serve_rate_low
     # error vs the FP64 oracle on a 1 % sample (one (time, channel) slice of
     # each sampled small request; the checker runs in the host-process pool)
     if pool is not None:
-        rng = np.random.default_rng(3)
-        small = [r for r in done if r.nsrc < 100_000]
-        pick = rng.choice(len(small), size=max(1, len(done) // 100), replace=False)
         errs = []
-        for k in pick:
-            r = small[k]
+        for r in done:
+            if r.rid not in kept:
+                continue
             sp = specs[r.set_id]
             g = np.random.default_rng(sp["seed"])
             full = serve.synth.hex_array(350, 14.6, 0.01, g)
@@ -517,7 +546,7 @@ def run_serve(args, device, pool):
             V = pool.apply(_cpu_worker, ((ant, float(f0), r.eq2tops[0].astype(np.float64),
                                           r.crd_eq.astype(np.float64),
                                           r.I_sky.astype(np.float64), bm),))[0]
-            errs.append(float(np.linalg.norm(r.result[0, 0] - V) / max(np.linalg.norm(V), 1e-300)))
+            errs.append(float(np.linalg.norm(kept[r.rid] - V) / max(np.linalg.norm(V), 1e-300)))
         out["sample_rel_err_max"] = max(errs)
         out["sample"] = f"{len(errs)} requests, slice (t=0, {sets[0].freqs[0] / 1e6:.0f} MHz)"
     for st in sets:

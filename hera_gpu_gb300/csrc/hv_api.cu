@@ -331,11 +331,14 @@ int dispatch_device(hv_context* ctx, int precision, int method, const void* antp
                             (const double*)I_sky, nsrc, (const double*)bm, P, out, st);
 }
 
+// Reads (and clears) the device error flag in stream order on the context's
+// stream: a copy on the legacy stream would wait on unrelated work.
 int check_err_flag(hv_context* ctx) {
   int flag = 0;
-  HV_CK(cudaMemcpy(&flag, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  HV_CK(cudaMemcpyAsync(&flag, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  HV_CK(cudaStreamSynchronize(ctx->stream));
   if (flag != 0) {
-    HV_CK(cudaMemset(ctx->d_err, 0, sizeof(int)));
+    HV_CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
     if (flag == 2)
       return fail(ctx, HV_ERR_ARG,
                   "antenna positions x frequency exceed the FP32 phase range of the tensor-core "

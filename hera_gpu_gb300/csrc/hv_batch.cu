@@ -440,12 +440,15 @@ int hv_batch_launch(hv_batch* b, void* stream) {
 
 int hv_batch_sync(hv_batch* b) {
   if (!b) return HV_ERR_ARG;
-  if (cudaStreamSynchronize(hv_context_stream(b->ctx)) != cudaSuccess) return HV_ERR_CUDA;
+  // the error flag is read in stream order on the batch's stream (a copy on
+  // the legacy stream would wait on the other streams' work)
+  cudaStream_t st = hv_context_stream(b->ctx);
   int flag = 0;
-  if (cudaMemcpy(&flag, b->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+  if (cudaMemcpyAsync(&flag, b->d_err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
     return HV_ERR_CUDA;
   if (flag) {
-    cudaMemset(b->d_err, 0, sizeof(int));
+    cudaMemsetAsync(b->d_err, 0, sizeof(int), st);
     return flag == 2 ? HV_ERR_ARG : HV_ERR_TIMEOUT;
   }
   return HV_OK;

@@ -79,6 +79,7 @@ class Request:
     nant: int = 0
     error: str = None               # why the request was not served
     cancelled: bool = False
+    delivered: bool = False         # result handed to the consumer callback
 
     def cancel(self):
         """Drop the request if it has not been admitted yet."""
@@ -86,7 +87,7 @@ class Request:
 
     @property
     def ok(self):
-        return self.result is not None and self.error is None
+        return self.error is None and (self.result is not None or self.delivered)
 
     @property
     def latency(self):
@@ -176,18 +177,27 @@ class Server:
         self.rings = [_PinnedRing(c) for c in contexts]
         self.max_held = 0.0  # largest device memory admitted at once (bytes)
 
+    def _staging_bytes(self, r):
+        rs = self.sets[r.set_id]
+        return (sum(getattr(r, n).nbytes + 256 for n in ("crd_eq", "I_sky", "eq2tops"))
+                + 8 * r.nfreq * r.ntimes * rs.nant * rs.nant + 256)
+
+    def reserve(self, requests, cap_bytes=2 << 30):
+        """Size every slot's page-locked staging for the ``max_batch``
+        largest of ``requests`` (at most ``cap_bytes``), so that serving
+        them allocates no page-locked memory."""
+        sizes = sorted((self._staging_bytes(r) for r in requests), reverse=True)
+        need = min(sum(sizes[:self.max_batch]), cap_bytes)
+        for ring in self.rings:
+            ring.reset(need)
+
     def _launch(self, slot, reqs):
         """Copy the requests' inputs in, launch their batch and queue the
         result copies, all on the slot's stream.  Returns the in-flight record,
         or None when the launch failed (the requests then carry the error)."""
         ctx = self.ctxs[slot]
         ring = self.rings[slot]
-        need = 0
-        for r in reqs:
-            rs = self.sets[r.set_id]
-            need += sum(getattr(r, n).nbytes + 256 for n in ("crd_eq", "I_sky", "eq2tops"))
-            need += 8 * r.nfreq * r.ntimes * rs.nant * rs.nant + 256
-        ring.reset(need)
+        ring.reset(sum(self._staging_bytes(r) for r in reqs))
         bufs, outs, sims = [], [], []
         nbytes = sum(request_bytes(r, self.sets[r.set_id].nant, self.sets[r.set_id].P)
                      for r in reqs)
@@ -226,9 +236,13 @@ class Server:
             ctx.d2h(out, s["vis_out"])
         return _InFlight(slot, batch, reqs, bufs, outs, nbytes)
 
-    def run(self, requests, clock=time.perf_counter, poll_s=2e-4):
+    def run(self, requests, clock=time.perf_counter, poll_s=2e-4, on_result=None):
         """Serve ``requests`` (sorted by arrival, seconds from now); returns
-        them with results and timings."""
+        them with timings.  Each result lands in the slot's page-locked
+        staging; by default it is copied into ``request.result``.  With
+        ``on_result(request, view)`` the consumer gets the staged result
+        itself instead (no host copy) and must copy what it keeps before
+        returning: the slot reuses the staging for its next batch."""
         requests = sorted(requests, key=lambda r: r.arrival)
         pending = collections.deque()
         inflight = {}
@@ -249,14 +263,16 @@ class Server:
                         err = None
                     except _native.HeraVisError as e:
                         err = f"batch failed: {e}"
+                    t = clock() - t0  # the results are in host memory
                     for r, out in zip(f.reqs, f.outs):
-                        if err is None:
+                        r.t_done = t
+                        if err is not None:
+                            r.error = err
+                        elif on_result is None:
                             r.result = out.copy()
                         else:
-                            r.error = err
-                    t = clock() - t0
-                    for r in f.reqs:
-                        r.t_done = t
+                            on_result(r, out)
+                            r.delivered = True
                     f.batch.close()
                     for b in f.buffers:
                         self.ctxs[slot].device_free(b)

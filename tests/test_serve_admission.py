@@ -134,3 +134,20 @@ def test_budget_bounds_memory_in_flight():
     srv, _ = run(reqs, budget=2.5 * one, slots=4, max_batch=8)
     assert all(r.ok for r in reqs)
     assert one <= srv.max_held <= 2.5 * one
+
+
+def test_results_handed_to_consumer_without_copy():
+    reqs = [request(i, 800 + i, arrival=0.0) for i in range(6)]
+    seen = {}
+
+    def consume(r, view):
+        seen[r.rid] = (view.shape, float(view.real.max()))
+
+    FakeBatch.launched = []
+    srv = serve.Server(fake_sets(), [FakeContext()], hbm_budget=1e9, max_batch=2,
+                       batch_factory=FakeBatch)
+    done = srv.run(reqs, on_result=consume)
+    assert sorted(seen) == [r.rid for r in reqs]
+    assert all(r.ok and r.delivered and r.result is None for r in done)
+    assert all(shape == (r.nfreq, r.ntimes, 20, 20) and mx == 1.0
+               for r in done for shape, mx in [seen[r.rid]])
