@@ -63,6 +63,8 @@ def parse_args():
                     help="a second serving run at this rate (0 = skip)")
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-max-batch", type=int, default=2)
+    ap.add_argument("--serve-only", action="store_true",
+                    help="run only the serving leg and print its summary (profiling runs)")
     return ap.parse_args()
 
 
@@ -93,35 +95,28 @@ def tc_chunk(nsrc, nslices, ngroups, num_sms):
     return (c + 31) // 32 * 32
 
 
-def tc_pairs_ncols(nant):
-    """Sum over antenna-block pairs I <= J of the MMA N of the pair."""
+def tc_groups(nant):
+    """The fused kernel's block-pair groups (hv_tc.cu make_groups): per group
+    its MMA N.  Pairs (I, J), (I, J + 1) share row block I; the pairs left
+    over at the end of a row, (I, nb - 1), are taken as (nb - 1, I) and
+    paired in ascending I."""
     nb = (nant + 127) // 128
-    tot = 0
+    ncols = [(min(128, nant - 128 * b) + 15) // 16 * 16 for b in range(nb)]
+    groups, singles = [], []
     for I in range(nb):
-        for J in range(I, nb):
-            tot += (min(128, nant - 128 * J) + 15) // 16 * 16
-    return tot
+        J = I
+        while J + 1 < nb:
+            groups.append(128 + ncols[J + 1])
+            J += 2
+        if J < nb:
+            singles.append(I)
+    for k in range(0, len(singles), 2):
+        groups.append(128 + ncols[singles[k + 1]] if k + 1 < len(singles) else ncols[singles[k]])
+    return groups
 
 
 def tc_num_groups(nant):
-    nb = (nant + 127) // 128
-    pairs_rows = [[(I, J) for J in range(I, nb)] for I in range(nb)]
-    groups, singles = 0, []
-    for row in pairs_rows:
-        groups += len(row) // 2
-        if len(row) % 2:
-            singles.append(row[-1])
-    used = [False] * len(singles)
-    for i in range(len(singles)):
-        if used[i]:
-            continue
-        used[i] = True
-        for k in range(i + 1, len(singles)):
-            if not used[k] and len({*singles[i], *singles[k]}) <= 3:
-                used[k] = True
-                break
-        groups += 1
-    return groups
+    return len(tc_groups(nant))
 
 
 # ------------------------------------------------------------------- clocks --
@@ -365,7 +360,7 @@ def run_ours(args):
         chunk = tc_chunk(S, T_PER_STEP * F, ng, num_sms)
         stages = sum(sum(math.ceil(min(chunk, su - k0) / 32) for k0 in range(0, su, chunk))
                      for su in s_up) * F
-        hw_flops = stages * 24 * 2 * 128 * 16 * tc_pairs_ncols(N)
+        hw_flops = stages * 24 * 2 * 128 * 16 * sum(tc_groups(N))
         peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
         traffic_unit = load_traffic()
         units = sum(s_up) * F
@@ -558,6 +553,9 @@ def main():
     args = parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.serve_only:
+        print(json.dumps({"serve": run_serve(args, 0, None)}), flush=True)
+        return 0
     return run_ours(args)
 
 

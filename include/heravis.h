@@ -188,7 +188,9 @@ int hv_vis_gpu_noalloc(const void* d_antpos, int nant, double freq,
 /* Device memory and copies ordered on the context's stream (stream-ordered
  * allocation, so freeing does not stall other streams); used by host code
  * that keeps inputs resident or serves requests.  kind: 1 host->device,
- * 2 device->host, 3 device->device. */
+ * 2 device->host, 3 device->device.  Replace the PyCUDA gpuarray.to_gpu /
+ * gpuarray.empty buffers, .set() uploads and driver.Stream of
+ * hera_gpu/vis.py:198-209,214. */
 int hv_device_alloc(hv_context* ctx, size_t bytes, void** ptr);
 int hv_device_free(hv_context* ctx, void* ptr);
 int hv_memcpy_async(hv_context* ctx, void* dst, const void* src, size_t bytes, int kind);
@@ -196,7 +198,8 @@ int hv_memcpy_async(hv_context* ctx, void* dst, const void* src, size_t bytes, i
  * work is pending; a negative hv_status on error. */
 int hv_stream_query(hv_context* ctx);
 
-/* Page-locked host memory for fast host<->device copies (cudaHostAlloc). */
+/* Page-locked host memory for fast host<->device copies (cudaHostAlloc);
+ * replaces the host download buffers of hera_gpu/vis.py:207-208. */
 int hv_host_alloc(hv_context* ctx, size_t bytes, void** ptr);
 int hv_host_free(hv_context* ctx, void* ptr);
 
