@@ -22,10 +22,11 @@
 //   source chunk goes to HBM and a separate kernel reduces the chunks in a
 //   fixed order (deterministic split-K over sources).
 //
-// Pipeline inside a CTA (576 threads)
-//   warp 16       TMA producer: 32 source records per stage, one 2-D
+// Pipeline inside a CTA (608 threads)
+//   warp 16       TMA producer: 16 source records per stage, one 2-D
 //                 cp.async.bulk.tensor into shared memory.
-//   warps 0-15    phasor generators: for each (slot, antenna row, 8 sources)
+//   warps 0-15    phasor generators, in two teams of 8 warps that take
+//                 alternate stages: for each (slot, antenna row, 8 sources)
 //                 the bilinear beam (4 coalesced gathers: lanes are
 //                 antennas), the phase in cycles reduced exactly in FP32
 //                 (phase_cycles32), sincos, v = A sqrt(I) e^{2 pi i phi},
@@ -33,14 +34,15 @@
 //                 128-byte-swizzled UMMA layout.  After the last stage of an
 //                 item they drain TMEM to the partial buffer (epilogue).
 //   warp 17       MMA issuer (one thread) and TMEM owner.
+//   warp 18       cluster mode: pushes this CTA's tiles to peer CTAs.
 //
-// Operand layout of one stage (32 sources, K = 64 BF16 per antenna row):
-//   the hi tiles of the stage's slots, one after the other, then their lo
-//   tiles (16 KB each: 128 rows x 128 bytes); within a tile
-//   K chunks of 16 bytes: [Re s0-7, Re s8-15, Im s0-7, Im s8-15,
-//                          Re s16-23, Re s24-31, Im s16-23, Im s24-31]
-//   so each MMA K-step (16 elements) holds either the real or the imaginary
-//   parts of 16 sources, and per K half h (16 sources):
+// Operand layout of one stage (16 sources): one tile per slot, the slots'
+// tiles side by side (16 KB each: 128 rows x 128 bytes, K = 64 BF16 per
+// antenna row), within a row the K chunks of 16 bytes
+//   [Re hi s0-7, Re hi s8-15, Im hi s0-7, Im hi s8-15,
+//    Re lo s0-7, Re lo s8-15, Im lo s0-7, Im lo s8-15]
+//   so each MMA K-step (16 elements) holds the real or the imaginary parts
+//   of the hi or the lo halves of the 16 sources, and per split product:
 //     ReV += ReA ReB^T + ImA ImB^T,   ImV += ImA ReB^T - ReA ImB^T
 //   (V[a,b] = sum_s v_a conj(v_b)); the minus sign is the instruction
 //   descriptor's negate-A bit.  Split BF16 keeps hi*hi + hi*lo + lo*hi.
@@ -61,12 +63,18 @@
 namespace hv {
 
 constexpr int TC_ROWS = 128;          // antennas per block = MMA M
-constexpr int TC_KS = 32;             // sources per stage
-constexpr int TC_HALF = 16384;        // one operand tile: 128 rows x 128 B
-constexpr int TC_SLOT = 2 * TC_HALF;  // hi + lo tiles of one block (bytes per slot and stage)
+constexpr int TC_KS = 16;             // sources per stage
+constexpr int TC_SLOT = 16384;        // one block's tile per stage: 128 rows x 128 B (hi and lo)
 constexpr int TC_REC = TC_KS * 32;    // bytes of source records per stage
+// Record stages: more than operand stages (they are small), so the TMA
+// producer runs further ahead and a generator warp finds its next records
+// loaded even while slower warps still hold earlier stages.
+constexpr int TC_NREC = 8;
 constexpr int TC_GEN_WARPS = 16;
 constexpr int TC_GEN_THREADS = TC_GEN_WARPS * 32;
+constexpr int TC_TEAM_WARPS = 8;  // generator warps per stage (two teams, alternate stages)
+constexpr int TC_TEAM_THREADS = TC_TEAM_WARPS * 32;
+constexpr int TC_MAX_STAGES = 8;
 constexpr int TC_PRODUCER_WARP = TC_GEN_WARPS;
 constexpr int TC_MMA_WARP = TC_GEN_WARPS + 1;
 constexpr int TC_PUSH_WARP = TC_GEN_WARPS + 2;  // cluster mode: pushes tiles to peer CTAs
@@ -342,31 +350,24 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint32_t a_lo, uint32_
       : "memory");
 }
 
-// The 24 MMAs of one group and one stage (32 sources): for each half of
-// the stage (16 sources) and each split product (hi hi, hi lo, lo hi),
+// The 12 MMAs of one group and one stage (16 sources): for each split
+// product (hi hi, hi lo, lo hi),
 //   ReV += ReA ReB + ImA ImB,   ImV += ImA ReB - ReA ImB,
 // with B the group's column blocks side by side (N up to 256).  a, b:
-// descriptor low words of the hi tiles of the row block and of the first
-// column block; the lo tiles follow lo_step (descriptor units) later.
-// first: the stage opens the item.
-__device__ __forceinline__ void issue_group(uint32_t d_re, uint32_t a, uint32_t b,
-                                            uint32_t lo_step, uint32_t idp, uint32_t idn,
-                                            bool first) {
+// descriptor low words of the row block's tile and of the first column
+// block's tile; along K, Re hi, Im hi, Re lo, Im lo are 32 bytes (2
+// descriptor units) apart.  first: the stage opens the item.
+__device__ __forceinline__ void issue_group(uint32_t d_re, uint32_t a, uint32_t b, uint32_t idp,
+                                            uint32_t idn, bool first) {
   const uint32_t d_im = d_re + 256;
-  const uint32_t A[2] = {a, a + lo_step};
-  const uint32_t B[2] = {b, b + lo_step};
 #pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const uint32_t kre = 4u * h, kim = 4u * h + 2u;  // K-steps of 32 bytes
-#pragma unroll
-    for (int pr = 0; pr < 3; ++pr) {
-      const uint32_t aa = A[pr == 2 ? 1 : 0], bb = B[pr == 1 ? 1 : 0];
-      const uint32_t acc = (first && h == 0 && pr == 0) ? 0u : 1u;
-      mma_bf16(d_re, aa + kre, bb + kre, idp, acc);
-      mma_bf16(d_re, aa + kim, bb + kim, idp, 1u);
-      mma_bf16(d_im, aa + kim, bb + kre, idp, acc);
-      mma_bf16(d_im, aa + kre, bb + kim, idn, 1u);
-    }
+  for (int pr = 0; pr < 3; ++pr) {
+    const uint32_t aa = a + (pr == 2 ? 4u : 0u), bb = b + (pr == 1 ? 4u : 0u);  // lo: 64 B on
+    const uint32_t acc = (first && pr == 0) ? 0u : 1u;
+    mma_bf16(d_re, aa, bb, idp, acc);            // Re Re
+    mma_bf16(d_re, aa + 2u, bb + 2u, idp, 1u);   // Im Im
+    mma_bf16(d_im, aa + 2u, bb, idp, acc);       // Im Re
+    mma_bf16(d_im, aa, bb + 2u, idn, 1u);        // -Re Im
   }
 }
 
@@ -572,21 +573,22 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
   const int NS = p.nstages;
   const uint32_t op_base = smem_u32(smem);
   const uint32_t stage_bytes = (uint32_t)p.max_slots * TC_SLOT;
-  const uint32_t lo_bytes = (uint32_t)p.max_slots * TC_HALF;  // hi tile -> lo tile
   uint8_t* rec_smem = smem + (size_t)NS * stage_bytes;
   const uint32_t rec_base = smem_u32(rec_smem);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(rec_smem + (size_t)NS * TC_REC);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(rec_smem + (size_t)TC_NREC * TC_REC);
   const uint32_t bar0 = smem_u32(bars);
   // barrier addresses
-  auto rec_full = [&](int s) { return bar0 + 8u * s; };
-  auto smem_full = [&](int s) { return bar0 + 8u * (NS + s); };
-  auto smem_empty = [&](int s) { return bar0 + 8u * (2 * NS + s); };
-  auto rec_empty = [&](int s) { return bar0 + 8u * (3 * NS + s); };
-  auto gen_done = [&](int s) { return bar0 + 8u * (4 * NS + s); };
-  const uint32_t acc_full = bar0 + 8u * (5 * NS);
+  // record stages r < TC_NREC, operand stages s < NS
+  auto rec_full = [&](int r) { return bar0 + 8u * r; };
+  auto rec_empty = [&](int r) { return bar0 + 8u * (TC_NREC + r); };
+  const uint32_t sbar0 = bar0 + 8u * (2 * TC_NREC);
+  auto smem_full = [&](int s) { return sbar0 + 8u * s; };
+  auto smem_empty = [&](int s) { return sbar0 + 8u * (NS + s); };
+  auto gen_done = [&](int s) { return sbar0 + 8u * (2 * NS + s); };
+  const uint32_t acc_full = sbar0 + 8u * (3 * NS);
   const uint32_t acc_empty = acc_full + 8;
   const uint32_t drain = acc_full + 16;
-  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 5 * NS + 3);
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2 * TC_NREC + 3 * NS + 3);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -600,14 +602,16 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
   // cluster mode: operand bytes this CTA receives from peers per stage
   const uint32_t recv_bytes = kCluster ? (uint32_t)__ldg(&mine->recv_slots) * TC_SLOT : 0u;
   if (threadIdx.x == 0) {
-    const int full_count = kCluster ? mine->full_count : TC_GEN_WARPS;
+    const int full_count = kCluster ? mine->full_count : TC_TEAM_WARPS;
     const int empty_count = kCluster ? mine->empty_count : 1;
+    for (int r = 0; r < TC_NREC; ++r) {
+      mbar_init(rec_full(r), 1);
+      mbar_init(rec_empty(r), TC_TEAM_WARPS);
+    }
     for (int s = 0; s < NS; ++s) {
-      mbar_init(rec_full(s), 1);
       mbar_init(smem_full(s), full_count);
       mbar_init(smem_empty(s), empty_count);
-      mbar_init(rec_empty(s), TC_GEN_WARPS);
-      mbar_init(gen_done(s), TC_GEN_WARPS);
+      mbar_init(gen_done(s), TC_TEAM_WARPS);
     }
     mbar_init(acc_full, 1);
     mbar_init(acc_empty, TC_GEN_THREADS);
@@ -638,6 +642,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
   if (warp < TC_GEN_WARPS) {
     // ------------------------------------------------ phasor generators --
     const int tid = threadIdx.x;
+    const int team = warp / TC_TEAM_WARPS;  // takes the stages with gs % 2 == team
     uint32_t gs = 0, ic = 0;
     ItemInfo d;
     for (long long it = it0; it < p.total_items; it += istep) {
@@ -657,17 +662,16 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       // the slots this CTA fills: all of its group's (no clusters) or the
       // ones it owns (cluster mode)
       const int nfill = kCluster ? nown : g_nslots;
-      // this thread's units (fixed for the item): u = tid + i * 512
-      int u_slot[3], u_sg[3], u_a[3];
+      // this thread's units (fixed for the item): antenna row `row` and
+      // sources 8 sg .. 8 sg + 7 of its team's stages, in each slot it fills
+      const int tt = tid & (TC_TEAM_THREADS - 1);
+      const int row = tt & (TC_ROWS - 1), sg = tt >> 7;
+      int u_slot[3], u_a[3];
       bool u_ok[3];
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
-        const int u = tid + i * TC_GEN_THREADS;
-        const int k = (u >> 7) % max(nfill, 1);
-        const int slot = kCluster ? __ldg(&gp->own_slot[min(k, 2)]) : k;
+        const int slot = kCluster ? __ldg(&gp->own_slot[i]) : i;
         u_slot[i] = slot;
-        u_sg[i] = (u >> 7) / max(nfill, 1);
-        const int row = u & (TC_ROWS - 1);
         const int srows = slot == 0 ? g_rows0 : (slot == 1 ? g_rows1 : g_rows2);
         const int sblk = slot == 0 ? g_blk0 : (slot == 1 ? g_blk1 : g_blk2);
         u_ok[i] = i < nfill && row < srows;
@@ -676,25 +680,21 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       // the phase coefficients of the first unit's antenna, fixed for the item
       Ucoef32 uc0 = {};
       if (u_ok[0]) uc0 = Us[u_a[0]];
-      const int row = tid & (TC_ROWS - 1);
       const int r8 = row & 7;
       const uint32_t rowoff = (uint32_t)(row >> 3) * 1024u + (uint32_t)r8 * 128u;
       const int wmask = kCluster ? __ldg(&gp->write_mask) : 1;
       bool ok = true;
       for (int j = 0; j < d.nst && ok && generates; ++j, ++gs) {
+        if ((int)(gs & 1u) != team) continue;  // the other team's stage
         const int s = (int)(gs % NS);
         const uint32_t par = (gs / NS) & 1;
-        if (!wait_warp(rec_full(s), par, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
+        const int rs = (int)(gs % TC_NREC);
+        if (!wait_warp(rec_full(rs), (gs / TC_NREC) & 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
         if (!wait_warp<kCluster>(smem_empty(s), par ^ 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
-        const SrcRec32* recs = reinterpret_cast<const SrcRec32*>(rec_smem + (size_t)s * TC_REC);
+        const SrcRec32* recs = reinterpret_cast<const SrcRec32*>(rec_smem + (size_t)rs * TC_REC);
         const uint32_t stage_op = op_base + (uint32_t)s * stage_bytes;
         auto unit = [&](int i) {
-          const int sg = u_sg[i];
-          const int h = sg >> 1, sub = sg & 1;
-          const uint32_t off_re = rowoff + ((uint32_t)((4 * h + sub) ^ r8) << 4);
-          const uint32_t off_im = rowoff + ((uint32_t)((4 * h + 2 + sub) ^ r8) << 4);
-          const uint32_t hi_tile = stage_op + (uint32_t)u_slot[i] * TC_HALF;
-          const uint32_t lo_tile = hi_tile + lo_bytes;
+          const uint32_t tile = stage_op + (uint32_t)u_slot[i] * TC_SLOT + rowoff;
           uint4 re_h = make_uint4(0, 0, 0, 0), im_h = re_h, re_l = re_h, im_l = re_h;
           if (u_ok[i]) {
             float rv[8], iv[8];
@@ -703,10 +703,10 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
             split_pack(rv, re_h, re_l);
             split_pack(iv, im_h, im_l);
           }
-          sts128(hi_tile + off_re, re_h);
-          sts128(hi_tile + off_im, im_h);
-          sts128(lo_tile + off_re, re_l);
-          sts128(lo_tile + off_im, im_l);
+          sts128(tile + ((uint32_t)(sg ^ r8) << 4), re_h);
+          sts128(tile + ((uint32_t)((2 + sg) ^ r8) << 4), im_h);
+          sts128(tile + ((uint32_t)((4 + sg) ^ r8) << 4), re_l);
+          sts128(tile + ((uint32_t)((6 + sg) ^ r8) << 4), im_l);
         };
         if (kCluster) {
           // static unit indices keep the unit tables in registers (a CTA that
@@ -726,7 +726,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
         if (lane == 0) {
           mbar_arrive(smem_full(s));
           if (kCluster) mbar_arrive(gen_done(s));
-          mbar_arrive(rec_empty(s));  // the records may be reloaded
+          mbar_arrive(rec_empty(rs));  // the records may be reloaded
         }
       }
       if (!ok) break;
@@ -783,21 +783,22 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       for (long long it = it0; it < p.total_items && ok; it += istep) {
         if (!decode_item<kCluster, kTable>(p, it, rank, d)) continue;
         for (int j = 0; j < d.nst; ++j, ++gs) {
-          const int s = (int)(gs % NS);
-          const uint32_t par = (gs / NS) & 1;
+          const int r = (int)(gs % TC_NREC);
+          const uint32_t par = (gs / TC_NREC) & 1;
           // this CTA's generators have finished reading the previous round
-          if (!wait1(rec_empty(s), par ^ 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
+          if (!wait1(rec_empty(r), par ^ 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
           // fault injection: stage 0 never fills, so its consumers time out
           if (p.stall && gs == 0) continue;
-          mbar_expect_tx(rec_full(s), TC_REC);
-          tma_load_2d(rec_base + (uint32_t)s * TC_REC, &rec_map, rec_full(s), 0,
+          mbar_expect_tx(rec_full(r), TC_REC);
+          tma_load_2d(rec_base + (uint32_t)r * TC_REC, &rec_map, rec_full(r), 0,
                       SIM_I(d, rec_row0) + d.tl * SIM_I(d, rec_stride) + d.s0 +
                           j * TC_KS);
         }
       }
       // let the copies still in flight land before the CTA can exit
-      const uint32_t first = gs > (uint32_t)NS ? gs - NS : 0;
-      for (uint32_t g = first; g < gs; ++g) wait_drain(rec_full((int)(g % NS)), (g / NS) & 1, p.err, p.wait_ns);
+      const uint32_t first = gs > (uint32_t)TC_NREC ? gs - TC_NREC : 0;
+      for (uint32_t g = first; g < gs; ++g)
+        wait_drain(rec_full((int)(g % TC_NREC)), (g / TC_NREC) & 1, p.err, p.wait_ns);
     }
   } else if (warp == TC_MMA_WARP) {
     // ------------------------------------------------------- MMA issuer --
@@ -811,9 +812,8 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
         const TcGroup* gp = SIM_P(d, groups) + d.g;
         const int nm = __ldg(&gp->n_mma);
         const uint32_t idp = idesc_bf16(nm, false), idn = idesc_bf16(nm, true);
-        const uint32_t a0 = desc_lo(op_base + (uint32_t)__ldg(&gp->sa) * TC_HALF);
+        const uint32_t a0 = desc_lo(op_base + (uint32_t)__ldg(&gp->sa) * TC_SLOT);
         const uint32_t b0 = desc_lo(op_base);
-        const uint32_t lo_step = lo_bytes >> 4;
         if (!wait1(acc_empty, (ic & 1) ^ 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
         tc_fence_after();
         for (int j = 0; j < d.nst; ++j, ++gs) {
@@ -825,7 +825,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
           if (recv_bytes) mbar_expect_tx(smem_full(s), recv_bytes);
           tc_fence_after();
           const uint32_t so = ((uint32_t)s * stage_bytes) >> 4;
-          issue_group(tmem, a0 + so, b0 + so, lo_step, idp, idn, j == 0);
+          issue_group(tmem, a0 + so, b0 + so, idp, idn, j == 0);
           // the stage's slots may be refilled -- here and, in cluster mode,
           // by the CTAs that wrote them -- once these MMAs have read them
           if (kCluster && cmask != (uint16_t)(1u << rank)) mma_commit_multicast(smem_empty(s), cmask);
@@ -854,14 +854,12 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
         if (!wait1(gen_done(s), par, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
         const uint32_t stage_op = op_base + (uint32_t)s * stage_bytes;
         for (int k = 0; k < nown; ++k) {
-          const uint32_t src = stage_op + (uint32_t)__ldg(&mine->own_slot[k]) * TC_HALF;
+          const uint32_t src = stage_op + (uint32_t)__ldg(&mine->own_slot[k]) * TC_SLOT;
           const int nd = __ldg(&mine->ndst[k]);
           for (int q = 0; q < nd; ++q) {
             const uint32_t rr = (uint32_t)__ldg(&mine->dst_rank[k][q]);
-            const uint32_t dst = stage_op + (uint32_t)__ldg(&mine->dst_slot[k][q]) * TC_HALF;
-            const uint32_t bar = map_to_rank(smem_full(s), rr);
-            bulk_push(map_to_rank(dst, rr), src, TC_HALF, bar);                        // hi
-            bulk_push(map_to_rank(dst + lo_bytes, rr), src + lo_bytes, TC_HALF, bar);  // lo
+            const uint32_t dst = stage_op + (uint32_t)__ldg(&mine->dst_slot[k][q]) * TC_SLOT;
+            bulk_push(map_to_rank(dst, rr), src, TC_SLOT, map_to_rank(smem_full(s), rr));
           }
         }
       }
@@ -988,7 +986,7 @@ void plan_cluster(std::vector<TcGroup>& gs, int nant) {
           for (int q = 0; q < gs[o].ndst[k]; ++q)
             if (gs[o].dst_rank[k][q] == x) ++recv;
     gs[x].recv_slots = recv;
-    gs[x].full_count = (gs[x].nown > 0 ? TC_GEN_WARPS : 0) + (recv > 0 ? 1 : 0);
+    gs[x].full_count = (gs[x].nown > 0 ? TC_TEAM_WARPS : 0) + (recv > 0 ? 1 : 0);
     (void)writers;
     gs[x].commit_mask = commit;
     gs[x].empty_count = 1 + targets;
@@ -1115,9 +1113,9 @@ cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, l
   p.err = err;
   p.wait_ns = wait_ns ? wait_ns : TC_WAIT_NS;
   p.stall = stall;
-  const int per_stage = p.max_slots * TC_SLOT + TC_REC;
-  const int fixed = 1024 /*alignment*/ + 512 /*barriers, holder*/;
-  p.nstages = std::min(4, (TC_SMEM_LIMIT - fixed) / per_stage);
+  const int per_stage = p.max_slots * TC_SLOT;
+  const int fixed = 1024 /*alignment*/ + TC_NREC * TC_REC + 512 /*barriers, holder*/;
+  p.nstages = std::min(TC_MAX_STAGES, (TC_SMEM_LIMIT - fixed) / per_stage);
   if (p.nstages < 2) return cudaErrorInvalidConfiguration;
   const int smem = fixed + p.nstages * per_stage;
   e = tc_configure();
@@ -1144,7 +1142,7 @@ cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, l
   cfg.gridDim = dim3((unsigned)(C * (num_sms / C)));
   // co-resident clusters for this cluster size and shared memory (cached:
   // the query is host-side and stays valid)
-  static int cached_n[2][TC_MAX_CLUSTER + 1][5] = {};
+  static int cached_n[2][TC_MAX_CLUSTER + 1][TC_MAX_STAGES + 1] = {};
   int& nclusters = cached_n[table][C][p.nstages];
   if (nclusters == 0) {
     e = table ? cudaOccupancyMaxActiveClusters(&nclusters, tc_vis_kernel<true, true>, &cfg)
