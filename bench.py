@@ -90,8 +90,9 @@ def sources_up(w, t):
 
 def tc_chunk(nsrc, nslices, ngroups, num_sms):
     """Split-K chunk the library picks (hv_tc.cu tc_chunk_sources)."""
-    want = nslices * ngroups * max(nsrc // 2, 1) // (8 * num_sms)
-    c = min(16384, max(1024, want))
+    nchunk = max(1, -(-40 * num_sms // (nslices * ngroups)))
+    c = -(-max(nsrc // 2, 1) // nchunk)
+    c = min(16384, max(1024, c))
     return (c + 31) // 32 * 32
 
 
@@ -358,9 +359,10 @@ def run_ours(args):
     if args.method == "tc":
         ng = tc_num_groups(N)
         chunk = tc_chunk(S, T_PER_STEP * F, ng, num_sms)
-        stages = sum(sum(math.ceil(min(chunk, su - k0) / 32) for k0 in range(0, su, chunk))
+        # 16-source stages of 12 MMAs (3 split products x 4 real products)
+        stages = sum(sum(math.ceil(min(chunk, su - k0) / 16) for k0 in range(0, su, chunk))
                      for su in s_up) * F
-        hw_flops = stages * 24 * 2 * 128 * 16 * sum(tc_groups(N))
+        hw_flops = stages * 12 * 2 * 128 * 16 * sum(tc_groups(N))
         peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
         traffic_unit = load_traffic()
         units = sum(s_up) * F

@@ -542,21 +542,33 @@ __device__ __forceinline__ bool decode_item(const TcParams& p, long long it, int
     d.sim = p.sims + lo;
     rest -= __ldg(&d.sim->item0);
   }
-  const int ngroups = SIM_I(d, ngroups), nchunk = SIM_I(d, nchunk), nf = SIM_I(d, nf);
+  // A simulation's items enumerate only the source chunks that hold sources
+  // above the horizon: per time t, chunks k < ceil(count_t / chunk), each for
+  // every frequency (and, without clusters, every group), chunk-major so
+  // that the short last chunk of a time comes last.  Item indices past the
+  // last such chunk (the host counts every chunk) decode to nothing.
+  const int ngroups = SIM_I(d, ngroups), nf = SIM_I(d, nf), nt = SIM_I(d, nt);
+  const int chunk = SIM_I(d, chunk);
+  const int* counts = SIM_P(d, counts);
   if (kCluster) {
     d.g = rank;
   } else {
     d.g = (int)(rest % ngroups);
     rest = rest / ngroups;
   }
-  d.k = (int)(rest % nchunk);
-  d.sl = (int)(rest / nchunk);
-  d.tl = d.sl / nf;
-  d.f = d.sl % nf;
-  const int cnt = __ldg(SIM_P(d, counts) + d.tl);
-  const int chunk = SIM_I(d, chunk);
+  int t = 0, cnt = 0;
+  for (; t < nt; ++t) {
+    cnt = __ldg(counts + t);
+    const long long n_t = (long long)((cnt + chunk - 1) / chunk) * nf;
+    if (rest < n_t) break;
+    rest -= n_t;
+  }
+  if (t >= nt) return false;
+  d.k = (int)(rest / nf);
+  d.f = (int)(rest % nf);
+  d.tl = t;
+  d.sl = t * nf + d.f;
   d.s0 = d.k * chunk;
-  if (d.s0 >= cnt) return false;
   d.s1 = min(d.s0 + chunk, cnt);
   d.nst = (d.s1 - d.s0 + TC_KS - 1) / TC_KS;
   return true;
@@ -1022,10 +1034,16 @@ int tc_fill_group_table(int nant, void* host_buf) {
 }
 
 int tc_chunk_sources(int nsrc, int nslices, int ngroups, int num_sms) {
-  // enough items to fill every SM a few times, chunks of 1k-16k sources
-  const long long want = (long long)nslices * ngroups * std::max(nsrc / 2, 1) / (8LL * num_sms);
-  long long c = std::min<long long>(16384, std::max<long long>(1024, want));
-  c = (c + TC_KS - 1) / TC_KS * TC_KS;
+  // about 40 items per cluster (or per CTA without clusters), so that the
+  // round-robin hand-out leaves a short tail, in chunks of 1k-16k sources
+  // (about half the catalogue is above the horizon)
+  const long long nchunk =
+      std::max<long long>(1, (40LL * num_sms + (long long)nslices * ngroups - 1) /
+                                 ((long long)nslices * ngroups));
+  const long long up = std::max(nsrc / 2, 1);
+  long long c = (up + nchunk - 1) / nchunk;
+  c = std::min<long long>(16384, std::max<long long>(1024, c));
+  c = (c + 31) / 32 * 32;
   return (int)c;
 }
 
