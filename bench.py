@@ -63,6 +63,10 @@ def parse_args():
                     help="a second serving run at this rate (0 = skip)")
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-max-batch", type=int, default=2)
+    ap.add_argument("--batch-sims", type=int, default=256,
+                    help="simulations of the batched-form leg (0 = skip)")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="run only the batched-form leg and print its summary")
     ap.add_argument("--serve-only", action="store_true",
                     help="run only the serving leg and print its summary (profiling runs)")
     return ap.parse_args()
@@ -463,6 +467,10 @@ def run_ours(args):
             errs[method] = float(np.linalg.norm(v - V_cpu) / np.linalg.norm(V_cpu))
         line["rel_err_vs_fp64"] = {**errs, "sample": f"{N} ant x {nsamp} src, one slice"}
 
+    # ---- batched form: many uneven simulations in one plan ----------------
+    if rank == 0 and args.batch_sims > 0:
+        line["batch"] = run_batch(args, local)
+
     # ---- serving: Poisson request stream, continuous batching --------------
     if rank == 0 and args.serve_requests > 0:
         line["serve"] = run_serve(args, local, pool)
@@ -474,6 +482,73 @@ def run_ours(args):
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def run_batch(args, device, steps=5, warmup=3):
+    """The batched-form configuration: --batch-sims simulations with nant
+    log-uniform in [16, 350] on random hex subsets, nsrc log-uniform in
+    [1e3, 2e5], ntimes uniform in [1, 60], nfreq uniform in [1, 16] over
+    100-200 MHz and beams of 31 or 63 pixels, planned as one batch (one
+    persistent fused launch per cluster class), split-K tuned on the batch,
+    captured as a CUDA graph and replayed.  Inputs are resident on the
+    device; a step is one replay, and its time includes every kernel of the
+    batch (source sort, preparation, fused launches, reductions)."""
+    import numpy as np
+    import torch
+    from hera_gpu_gb300 import _native, synth
+    dev = torch.device("cuda", device)
+    specs = synth.config_batch(seed=0, nsims=args.batch_sims)
+    keep, sims = [], []
+    for sp in specs:
+        arrs, dish = synth.make_sim_arrays(sp)
+        d = {k: torch.from_numpy(np.ascontiguousarray(arrs[k])).to(dev)
+             for k in ("antpos", "eq2tops", "crd_eq", "I_sky")}
+        # Airy power beams (2 J1(x)/x)^2, x = pi D sin(theta) / lambda, as
+        # synth.airy_beams, evaluated on the device
+        g = torch.linspace(-1.0, 1.0, sp["P"], dtype=torch.float64, device=dev)
+        st = torch.clamp(torch.hypot(g[None, :], g[:, None]), max=1.0)
+        dsh = torch.from_numpy(dish).to(dev)
+        lam = synth.C_LIGHT / torch.from_numpy(arrs["freqs"]).to(dev)
+        x = torch.pi * dsh[None, :, None, None] * st[None, None] / lam[:, None, None, None]
+        safe = torch.where(x == 0, torch.ones_like(x), x)
+        bm = torch.where(x == 0, torch.ones_like(x), (2 * torch.special.bessel_j1(safe) / safe) ** 2)
+        d["bm_cubes"] = bm.to(torch.float32).contiguous()
+        d["out"] = torch.empty((len(arrs["freqs"]), sp["ntimes"], sp["nant"], sp["nant"]),
+                               dtype=torch.complex64, device=dev)
+        keep.append(d)
+        sims.append(dict(antpos=d["antpos"].data_ptr(), eq2tops=d["eq2tops"].data_ptr(),
+                         crd_eq=d["crd_eq"].data_ptr(), I_sky=d["I_sky"].data_ptr(),
+                         bm_cubes=d["bm_cubes"].data_ptr(), freqs=arrs["freqs"],
+                         vis_out=d["out"].data_ptr(), nant=sp["nant"], ntimes=sp["ntimes"],
+                         nsrc=sp["nsrc"], beam_px=sp["P"]))
+    torch.cuda.synchronize(dev)
+    ctx = _native.Context(device)
+    t0 = time.perf_counter()
+    b = _native.Batch(ctx, sims, graph=True, autotune=True)
+    plan_s = time.perf_counter() - t0
+    stream = torch.cuda.Stream(dev)
+    for _ in range(warmup):
+        b.launch(stream.cuda_stream)
+    stream.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        b.launch(stream.cuda_stream)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    b.sync()
+    vis = sum(sp["nfreq"] * sp["ntimes"] * sp["nant"] ** 2 for sp in specs)
+    out = {"sims": len(specs), "vis_per_step": vis, "ms_per_step": ms,
+           "vis_per_s": vis / (ms / 1e3), "unit": "vis/s", "steps": steps, "warmup": warmup,
+           "graph": True, "autotune": True, "plan_s": plan_s,
+           "gpu_launches_per_step": b.launches,
+           "workload": "nant logU[16,350] hex subsets, nsrc logU[1e3,2e5], ntimes U[1,60], "
+                       "nfreq U[1,16] 100-200 MHz, P in {31,63}; inputs resident"}
+    b.close()
+    del keep
+    torch.cuda.empty_cache()
+    return out
 
 
 def run_serve(args, device, pool):
@@ -557,6 +632,9 @@ def main():
         return run_reference(args)
     if args.serve_only:
         print(json.dumps({"serve": run_serve(args, 0, None)}), flush=True)
+        return 0
+    if args.batch_only:
+        print(json.dumps({"batch": run_batch(args, 0)}), flush=True)
         return 0
     return run_ours(args)
 

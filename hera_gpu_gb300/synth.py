@@ -149,10 +149,9 @@ def config_batch(seed=0, nsims=256):
     return sims
 
 
-def make_sim(spec, dtype=np.float32):
-    """Arrays for one simulation of :func:`config_batch`: antennas on a random
-    subset of the 350-element hex grid, sphere-uniform power-law sources,
-    Airy beams, frequencies evenly spaced in 100-200 MHz."""
+def make_sim_arrays(spec, dtype=np.float32):
+    """Everything of :func:`make_sim` but the beam cubes: the arrays, and the
+    per-antenna dish diameters the Airy beams are made from."""
     rng = np.random.default_rng(spec["seed"])
     full = hex_array(350, 14.6, 0.01, rng)
     pick = np.sort(rng.choice(350, size=spec["nant"], replace=False))
@@ -162,10 +161,19 @@ def make_sim(spec, dtype=np.float32):
     nf = spec["nfreq"]
     freqs = np.linspace(100e6, 200e6, nf) if nf > 1 else np.array([150e6])
     dish = 14.0 * (1.0 + 0.02 * rng.uniform(-1.0, 1.0, spec["nant"]))
-    bm = np.empty((nf, spec["nant"], spec["P"], spec["P"]), dtype=dtype)
-    for i, f in enumerate(freqs):
-        bm[i] = airy_beams(spec["nant"], spec["P"], f, dish)
     lsts = sky.lst_grid(spec["ntimes"], 1.0, start_rad=rng.uniform(0, 2 * np.pi))
     e2t = sky.eq2tops(lsts, np.radians(sky.HERA_LATITUDE_DEG))
     return dict(antpos=antpos.astype(dtype), freqs=freqs, eq2tops=e2t.astype(dtype),
-                crd_eq=crd_eq.astype(dtype), I_sky=I_sky.astype(dtype), bm_cubes=bm)
+                crd_eq=crd_eq.astype(dtype), I_sky=I_sky.astype(dtype)), dish
+
+
+def make_sim(spec, dtype=np.float32):
+    """Arrays for one simulation of :func:`config_batch`: antennas on a random
+    subset of the 350-element hex grid, sphere-uniform power-law sources,
+    Airy beams, frequencies evenly spaced in 100-200 MHz."""
+    sim, dish = make_sim_arrays(spec, dtype)
+    bm = np.empty((len(sim["freqs"]), spec["nant"], spec["P"], spec["P"]), dtype=dtype)
+    for i, f in enumerate(sim["freqs"]):
+        bm[i] = airy_beams(spec["nant"], spec["P"], f, dish)
+    sim["bm_cubes"] = bm
+    return sim
