@@ -42,6 +42,9 @@ struct hv_context {
   int num_sms = 0;
   int cc_major = 0, cc_minor = 0;
   cudaStream_t stream = nullptr;
+  // a fused launch of one simulation shared between its cluster kernel and a
+  // one-CTA kernel on the SMs no cluster fits on (launch_tc_batch)
+  hv::TcShare share{};
   size_t budget = 0;  // 0 = unlimited
   size_t held = 0;
   std::string err;
@@ -284,8 +287,10 @@ int run_device(hv_context* ctx, int method, const R* antpos, int nant, const dou
         if (nsrc > 0)
           HV_LAUNCH_TIMED(launch_tc_batch(&L, 1, ctx->rec.p, (long long)nt * rec_stride,
                                           ctx->tctable.p, ctx->tctable_h.p, ctx->d_err,
-                                          ctx->num_sms, st, ctx->wait_ns, ctx->stall),
+                                          ctx->num_sms, st, ctx->wait_ns, ctx->stall,
+                                          &ctx->share),
                           st);
+        if (nsrc > 0 && ctx->share.launched > 1) ctx->launches += ctx->share.launched - 1;
         HV_LAUNCH(1, launch_reduce<float>(static_cast<float*>(ctx->partial.p), slice_floats,
                                           counts + t0, nt, nfreq, t0, ntimes, chunk, Np, nant,
                                           out, st));
@@ -418,8 +423,20 @@ int hv_create(hv_context** out, int device, size_t hbm_budget_bytes) {
     ctx->cc_major = prop.major;
     ctx->cc_minor = prop.minor;
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { r = HV_ERR_CUDA; break; }
-    if (cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess) { r = HV_ERR_OOM; break; }
-    if (cudaMemset(ctx->d_err, 0, sizeof(int)) != cudaSuccess) { r = HV_ERR_CUDA; break; }
+    // device error flag and the split point of shared fused launches
+    if (cudaMalloc(&ctx->d_err, 2 * sizeof(int)) != cudaSuccess) { r = HV_ERR_OOM; break; }
+    if (cudaMemset(ctx->d_err, 0, 2 * sizeof(int)) != cudaSuccess) { r = HV_ERR_CUDA; break; }
+    ctx->share.d_split = ctx->d_err + 1;
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&ctx->share.hi, cudaStreamNonBlocking, greatest) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&ctx->share.lo, cudaStreamNonBlocking, least) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->share.fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->share.join_hi, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->share.join_lo, cudaEventDisableTiming) != cudaSuccess) {
+      r = HV_ERR_CUDA;
+      break;
+    }
     // keep freed stream-ordered memory in the pool for reuse
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
@@ -451,8 +468,14 @@ int hv_destroy(hv_context* ctx) {
     cudaEventDestroy(ev.first);
     cudaEventDestroy(ev.second);
   }
+  if (ctx->share.hi) cudaStreamSynchronize(ctx->share.hi);
+  if (ctx->share.lo) cudaStreamSynchronize(ctx->share.lo);
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->share.hi) cudaStreamDestroy(ctx->share.hi);
+  if (ctx->share.lo) cudaStreamDestroy(ctx->share.lo);
+  for (cudaEvent_t ev : {ctx->share.fork, ctx->share.join_hi, ctx->share.join_lo})
+    if (ev) cudaEventDestroy(ev);
   delete ctx;
   return HV_OK;
 }

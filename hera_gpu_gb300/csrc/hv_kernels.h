@@ -110,9 +110,19 @@ cudaError_t tc_configure();
 // simulation has the same clusterable group layout.  wait_ns: limit of
 // each device-side wait (0: 2 s); stall: fault injection (the first record
 // copy is never issued, so the launch ends with a timeout status).
+// share (one simulation in cluster mode): the SMs no cluster fits on run a
+// share of the items in a second, concurrent launch (forked from st onto
+// share->hi / share->lo and joined back); share->launched counts kernels.
+struct TcShare {
+  cudaStream_t hi, lo;                  // highest- and lowest-priority streams
+  cudaEvent_t fork, join_hi, join_lo;   // timing disabled
+  int* d_split;                         // device int: the split point
+  int launched;
+};
 cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, long long rec_rows,
                             void* d_table, void* h_table, int* err, int num_sms,
-                            cudaStream_t st, unsigned long long wait_ns = 0, int stall = 0);
+                            cudaStream_t st, unsigned long long wait_ns = 0, int stall = 0,
+                            TcShare* share = nullptr);
 size_t tc_partial_floats(int Np, int nsrc, int nslices, int chunk);
 int tc_chunk_sources(int nsrc, int nslices, int ngroups, int num_sms);
 size_t tc_group_table_bytes(int nant);

@@ -140,6 +140,11 @@ struct TcParams {
   int* err;
   unsigned long long wait_ns;  // limit of one wait
   int stall;                   // fault injection: the first record copy is never issued
+  // Shared launch of one simulation (split != null): the cluster launch runs
+  // the cluster items [0, *split), a one-CTA-per-item launch on the SMs no
+  // cluster fits on runs the group items [*split * ngroups, total_items).
+  const int* split;
+  int split_side;  // 0: the cluster launch, 1: the one-CTA launch
 };
 
 // Read-only load of a pointer-valued field.
@@ -608,8 +613,14 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
   // cluster mode: every simulation of the launch has the same group layout
   // (one group per CTA of the cluster), so its barrier counts are common
   const int csize = kCluster ? (kTable ? (int)__ldg(&p.sims[0].ngroups) : p.one.ngroups) : 1;
-  const long long it0 = kCluster ? blockIdx.x / csize : blockIdx.x;
+  long long it0 = kCluster ? blockIdx.x / csize : blockIdx.x;
   const long long istep = kCluster ? gridDim.x / csize : gridDim.x;
+  long long it_end = p.total_items;
+  if (p.split) {
+    const long long x = *p.split;
+    if (p.split_side) it0 += x * p.one.ngroups;
+    else it_end = min(it_end, x);
+  }
   const TcGroup* mine = (kTable ? ldg_ptr(&p.sims[0].groups) : p.one.groups) + rank;
   // cluster mode: operand bytes this CTA receives from peers per stage
   const uint32_t recv_bytes = kCluster ? (uint32_t)__ldg(&mine->recv_slots) * TC_SLOT : 0u;
@@ -657,7 +668,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
     const int team = warp / TC_TEAM_WARPS;  // takes the stages with gs % 2 == team
     uint32_t gs = 0, ic = 0;
     ItemInfo d;
-    for (long long it = it0; it < p.total_items; it += istep) {
+    for (long long it = it0; it < it_end; it += istep) {
       if (!decode_item<kCluster, kTable>(p, it, rank, d)) continue;
       const TcGroup* gp = SIM_P(d, groups) + d.g;
       const int Np = SIM_I(d, Np), dx = SIM_I(d, dx), dy = SIM_I(d, dy);
@@ -792,7 +803,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       uint32_t gs = 0;
       ItemInfo d;
       bool ok = true;
-      for (long long it = it0; it < p.total_items && ok; it += istep) {
+      for (long long it = it0; it < it_end && ok; it += istep) {
         if (!decode_item<kCluster, kTable>(p, it, rank, d)) continue;
         for (int j = 0; j < d.nst; ++j, ++gs) {
           const int r = (int)(gs % TC_NREC);
@@ -819,7 +830,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       ItemInfo d;
       bool ok = true;
       const uint16_t cmask = kCluster ? (uint16_t)__ldg(&mine->commit_mask) : (uint16_t)1;
-      for (long long it = it0; it < p.total_items && ok; it += istep) {
+      for (long long it = it0; it < it_end && ok; it += istep) {
         if (!decode_item<kCluster, kTable>(p, it, rank, d)) continue;
         const TcGroup* gp = SIM_P(d, groups) + d.g;
         const int nm = __ldg(&gp->n_mma);
@@ -858,7 +869,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
     uint32_t gs = 0;
     ItemInfo d;
     bool ok = true;
-    for (long long it = it0; it < p.total_items && ok; it += istep) {
+    for (long long it = it0; it < it_end && ok; it += istep) {
       if (!decode_item<kCluster, kTable>(p, it, rank, d)) continue;
       for (int j = 0; j < d.nst; ++j, ++gs) {
         const int s = (int)(gs % NS);
@@ -894,6 +905,18 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
 
 #undef SIM_I
 #undef SIM_P
+
+// Where a shared launch of one simulation splits its items: the cluster
+// launch keeps the first (1 - side_frac) of the cluster items that hold
+// sources above the horizon (the decode order of decode_item).
+__global__ void tc_split_kernel(const int* __restrict__ counts, int nt, int nf, int chunk,
+                                float side_frac, int* __restrict__ split) {
+  if (threadIdx.x != 0) return;
+  long long n = 0;
+  for (int t = 0; t < nt; ++t) n += (long long)((counts[t] + chunk - 1) / chunk) * nf;
+  const long long side = (long long)ceilf(side_frac * (float)n);
+  *split = (int)(n - min(side, n));
+}
 
 // ------------------------------------------------------------------- host --
 namespace {
@@ -1066,7 +1089,9 @@ cudaError_t tc_configure() {
 
 cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, long long rec_rows,
                             void* d_table, void* h_table, int* err, int num_sms,
-                            cudaStream_t st, unsigned long long wait_ns, int stall) {
+                            cudaStream_t st, unsigned long long wait_ns, int stall,
+                            TcShare* share) {
+  if (share) share->launched = 0;
   if (nsims <= 0 || rec_rows <= 0) return cudaSuccess;
   auto encode = encode_fn();
   if (!encode) return cudaErrorNotSupported;
@@ -1170,9 +1195,41 @@ cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, l
   if (nclusters < 1) return cudaErrorInvalidConfiguration;
   const int ncl = (int)std::min<long long>(nclusters, items);
   cfg.gridDim = dim3((unsigned)(C * ncl));
+  const int leftover = num_sms - C * ncl;
+  if (share && !table && leftover >= 4) {
+    // The SMs no cluster fits on take a share of the items, one CTA per group
+    // item: a one-CTA item runs at about 0.55 of a cluster CTA's rate (it
+    // generates all of its group's blocks itself).  The cluster launch goes
+    // to the higher-priority stream so that its clusters are placed first.
+    const float r = 0.55f;
+    const float side_frac = leftover * r / (C * ncl + leftover * r);
+    const TcSimDesc& L = sims[0];
+    tc_split_kernel<<<1, 32, 0, st>>>(L.counts, L.nt, L.nf, L.chunk, side_frac, share->d_split);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if ((e = cudaEventRecord(share->fork, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(share->hi, share->fork, 0)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(share->lo, share->fork, 0)) != cudaSuccess) return e;
+    p.split = share->d_split;
+    p.split_side = 0;
+    cfg.stream = share->hi;
+    if ((e = cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, false>, map, p)) != cudaSuccess) return e;
+    TcParams q = p;
+    q.total_items = items * C;
+    q.split_side = 1;
+    tc_vis_kernel<false, false><<<leftover, TC_THREADS, smem, share->lo>>>(map, q);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(share->join_hi, share->hi)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(share->join_lo, share->lo)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(st, share->join_hi, 0)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(st, share->join_lo, 0)) != cudaSuccess) return e;
+    share->launched = 3;
+    return cudaSuccess;
+  }
   e = table ? cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, true>, map, p)
             : cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, false>, map, p);
   if (e != cudaSuccess) return e;
+  if (share) share->launched = 1;
   return cudaGetLastError();
 }
 
