@@ -340,7 +340,9 @@ int hv_batch_create(hv_context* ctx, const hv_sim* sims, int nsims, unsigned fla
       s.in = sims[i];
       s.ngroups = hv::tc_num_groups(sims[i].nant);
       s.max_slots = hv::tc_max_slots(sims[i].nant);
-      const int key = (s.ngroups > 1 && s.ngroups <= 8) ? s.ngroups : 0;
+      // cluster classes by cluster size; the others by generator team size
+      const int key = (s.ngroups > 1 && s.ngroups <= 8) ? s.ngroups
+                                                        : 100 + hv::tc_team_warps(sims[i].nant);
       auto it = class_of.find(key);
       if (it == class_of.end()) {
         class_of[key] = (int)b->classes.size();

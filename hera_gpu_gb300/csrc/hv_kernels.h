@@ -101,6 +101,9 @@ struct TcSimDesc {
 };
 size_t tc_sim_table_bytes(int nsims);
 int tc_num_groups(int nant);
+// Generator warps per stage of the fused kernel for nant antennas (launches
+// whose simulations differ use the largest).
+int tc_team_warps(int nant);
 // One-time launch attributes of the fused kernel (call outside stream capture).
 cudaError_t tc_configure();
 // All items of nsims simulations in one persistent launch.  rec: SrcRec32

@@ -72,8 +72,10 @@ constexpr int TC_REC = TC_KS * 32;    // bytes of source records per stage
 constexpr int TC_NREC = 8;
 constexpr int TC_GEN_WARPS = 16;
 constexpr int TC_GEN_THREADS = TC_GEN_WARPS * 32;
-constexpr int TC_TEAM_WARPS = 8;  // generator warps per stage (two teams, alternate stages)
-constexpr int TC_TEAM_THREADS = TC_TEAM_WARPS * 32;
+// Generator warps per stage: 8 (two teams on alternate stages); one-slot
+// launches of up to 64 (32) antennas use teams of 4 (2) warps, enough for
+// their rows, so that 4 (8) stages are generated at once.
+constexpr int TC_TEAM_WARPS = 8;
 constexpr int TC_MAX_STAGES = 8;
 constexpr int TC_PRODUCER_WARP = TC_GEN_WARPS;
 constexpr int TC_MMA_WARP = TC_GEN_WARPS + 1;
@@ -145,6 +147,7 @@ struct TcParams {
   // cluster fits on runs the group items [*split * ngroups, total_items).
   const int* split;
   int split_side;  // 0: the cluster launch, 1: the one-CTA launch
+  int team_warps;  // generator warps per stage (8, or 4 / 2 for small one-slot groups)
 };
 
 // Read-only load of a pointer-valued field.
@@ -625,16 +628,16 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
   // cluster mode: operand bytes this CTA receives from peers per stage
   const uint32_t recv_bytes = kCluster ? (uint32_t)__ldg(&mine->recv_slots) * TC_SLOT : 0u;
   if (threadIdx.x == 0) {
-    const int full_count = kCluster ? mine->full_count : TC_TEAM_WARPS;
+    const int full_count = kCluster ? mine->full_count : p.team_warps;
     const int empty_count = kCluster ? mine->empty_count : 1;
     for (int r = 0; r < TC_NREC; ++r) {
       mbar_init(rec_full(r), 1);
-      mbar_init(rec_empty(r), TC_TEAM_WARPS);
+      mbar_init(rec_empty(r), p.team_warps);
     }
     for (int s = 0; s < NS; ++s) {
       mbar_init(smem_full(s), full_count);
       mbar_init(smem_empty(s), empty_count);
-      mbar_init(gen_done(s), TC_TEAM_WARPS);
+      mbar_init(gen_done(s), p.team_warps);
     }
     mbar_init(acc_full, 1);
     mbar_init(acc_empty, TC_GEN_THREADS);
@@ -665,7 +668,9 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
   if (warp < TC_GEN_WARPS) {
     // ------------------------------------------------ phasor generators --
     const int tid = threadIdx.x;
-    const int team = warp / TC_TEAM_WARPS;  // takes the stages with gs % 2 == team
+    const int team_warps = kCluster ? TC_TEAM_WARPS : p.team_warps;
+    const int nteams = TC_GEN_WARPS / team_warps;
+    const int team = warp / team_warps;  // takes the stages with gs % nteams == team
     uint32_t gs = 0, ic = 0;
     ItemInfo d;
     for (long long it = it0; it < it_end; it += istep) {
@@ -687,8 +692,9 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       const int nfill = kCluster ? nown : g_nslots;
       // this thread's units (fixed for the item): antenna row `row` and
       // sources 8 sg .. 8 sg + 7 of its team's stages, in each slot it fills
-      const int tt = tid & (TC_TEAM_THREADS - 1);
-      const int row = tt & (TC_ROWS - 1), sg = tt >> 7;
+      const int tt = tid & (team_warps * 32 - 1);
+      const int nrows = team_warps * 16;  // rows a team covers (the block's valid rows)
+      const int row = tt % nrows, sg = tt / nrows;
       int u_slot[3], u_a[3];
       bool u_ok[3];
 #pragma unroll
@@ -708,7 +714,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       const int wmask = kCluster ? __ldg(&gp->write_mask) : 1;
       bool ok = true;
       for (int j = 0; j < d.nst && ok && generates; ++j, ++gs) {
-        if ((int)(gs & 1u) != team) continue;  // the other team's stage
+        if ((int)(gs % (uint32_t)nteams) != team) continue;  // another team's stage
         const int s = (int)(gs % NS);
         const uint32_t par = (gs / NS) & 1;
         const int rs = (int)(gs % TC_NREC);
@@ -1047,6 +1053,8 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 
 int tc_num_groups(int nant) { return (int)make_groups(nant).size(); }
 
+int tc_team_warps(int nant) { return nant <= 32 ? 2 : nant <= 64 ? 4 : TC_TEAM_WARPS; }
+
 size_t tc_group_table_bytes(int nant) { return sizeof(TcGroup) * make_groups(nant).size(); }
 
 int tc_fill_group_table(int nant, void* host_buf) {
@@ -1108,10 +1116,11 @@ cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, l
 
   // cluster mode when every simulation has the same (clusterable) group layout
   bool cluster = use_cluster(sims[0].ngroups);
-  int max_slots = 1;
+  int max_slots = 1, team_warps = 2;
   for (int i = 0; i < nsims; ++i) {
     if (sims[i].ngroups != sims[0].ngroups) cluster = false;
     max_slots = std::max(max_slots, sims[i].max_slots);
+    team_warps = std::max(team_warps, tc_team_warps(sims[i].nant));
   }
   TcSim* tab = static_cast<TcSim*>(h_table);
   long long items = 0;
@@ -1156,6 +1165,7 @@ cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, l
   p.err = err;
   p.wait_ns = wait_ns ? wait_ns : TC_WAIT_NS;
   p.stall = stall;
+  p.team_warps = team_warps;
   const int per_stage = p.max_slots * TC_SLOT;
   const int fixed = 1024 /*alignment*/ + TC_NREC * TC_REC + 512 /*barriers, holder*/;
   p.nstages = std::min(TC_MAX_STAGES, (TC_SMEM_LIMIT - fixed) / per_stage);
@@ -1198,10 +1208,11 @@ cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, l
   const int leftover = num_sms - C * ncl;
   if (share && !table && leftover >= 4) {
     // The SMs no cluster fits on take a share of the items, one CTA per group
-    // item: a one-CTA item runs at about 0.55 of a cluster CTA's rate (it
-    // generates all of its group's blocks itself).  The cluster launch goes
-    // to the higher-priority stream so that its clusters are placed first.
-    const float r = 0.55f;
+    // item: a one-CTA item runs at about 0.7 of a cluster CTA's rate (it
+    // generates all of its group's blocks itself; measured at 350 antennas).
+    // The cluster launch goes to the higher-priority stream so that its
+    // clusters are placed first.
+    const float r = 0.68f;
     const float side_frac = leftover * r / (C * ncl + leftover * r);
     const TcSimDesc& L = sims[0];
     tc_split_kernel<<<1, 32, 0, st>>>(L.counts, L.nt, L.nf, L.chunk, side_frac, share->d_split);
