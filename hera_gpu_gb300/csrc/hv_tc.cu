@@ -912,6 +912,14 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
 #undef SIM_I
 #undef SIM_P
 
+// Holds back the next launch on its stream by `ns` nanoseconds (one thread
+// timing itself; it waits on nothing else): the one-CTA launch of a shared
+// launch must not take SMs before the cluster launch has placed its clusters.
+__global__ void tc_hold_kernel(unsigned long long ns) {
+  const unsigned long long t0 = global_ns();
+  while (global_ns() - t0 < ns) __nanosleep(1000);
+}
+
 // Where a shared launch of one simulation splits its items: the cluster
 // launch keeps the first (1 - side_frac) of the cluster items that hold
 // sources above the horizon (the decode order of decode_item).
@@ -1228,13 +1236,14 @@ cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, l
     TcParams q = p;
     q.total_items = items * C;
     q.split_side = 1;
+    tc_hold_kernel<<<1, 32, 0, share->lo>>>(100000ull);
     tc_vis_kernel<false, false><<<leftover, TC_THREADS, smem, share->lo>>>(map, q);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = cudaEventRecord(share->join_hi, share->hi)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(share->join_lo, share->lo)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(st, share->join_hi, 0)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(st, share->join_lo, 0)) != cudaSuccess) return e;
-    share->launched = 3;
+    share->launched = 4;
     return cudaSuccess;
   }
   e = table ? cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, true>, map, p)
