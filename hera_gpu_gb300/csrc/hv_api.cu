@@ -395,6 +395,7 @@ void hv_context_record_kernel(hv_context* ctx, cudaEvent_t e0, cudaEvent_t e1) {
 
 bool hv_context_profiling(hv_context* ctx) { return ctx->profiling; }
 uint64_t hv_context_wait_ns(hv_context* ctx) { return ctx->wait_ns; }
+hv::TcShare* hv_context_share(hv_context* ctx) { return &ctx->share; }
 int hv_context_stall(hv_context* ctx) { return ctx->stall; }
 
 extern "C" {

@@ -278,9 +278,14 @@ int enqueue(hv_batch* b, cudaStream_t st, int timed_class = -1) {
         HB_CK(cudaEventCreate(&e1));
         HB_CK(cudaEventRecord(e0, st));
       }
+      // a class of one simulation in cluster mode shares its launch with the
+      // SMs no cluster fits on (not while timing split-K candidates)
+      TcShare* share = d.size() == 1 && timed_class < 0 ? hv_context_share(b->ctx) : nullptr;
       HB_CK(launch_tc_batch(d.data(), (int)d.size(), b->rec, b->rec_rows,
                             static_cast<char*>(b->table) + toff, H + b->h_table + toff, b->d_err,
-                            b->num_sms, st, hv_context_wait_ns(b->ctx), hv_context_stall(b->ctx)));
+                            b->num_sms, st, hv_context_wait_ns(b->ctx), hv_context_stall(b->ctx),
+                            share));
+      if (share && share->launched > 1) nl += share->launched - 1;
       if (prof) {
         HB_CK(cudaEventRecord(e1, st));
         hv_context_record_kernel(b->ctx, e0, e1);

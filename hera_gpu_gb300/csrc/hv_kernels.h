@@ -150,4 +150,6 @@ bool hv_context_profiling(hv_context* ctx);
 void hv_context_record_kernel(hv_context* ctx, cudaEvent_t e0, cudaEvent_t e1);
 // Wait limit and fault injection of the fused kernel (hv_set_wait_limit).
 uint64_t hv_context_wait_ns(hv_context* ctx);
+// Streams and scratch of the context for shared fused launches (TcShare).
+hv::TcShare* hv_context_share(hv_context* ctx);
 int hv_context_stall(hv_context* ctx);
