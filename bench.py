@@ -234,6 +234,23 @@ def dist_setup():
     return world, rank, local
 
 
+def max_over_ranks(x, device=None):
+    """The largest of every rank's x (the job's time is its slowest
+    replica's); x itself without a process group."""
+    import torch
+    if not (torch.distributed.is_available() and torch.distributed.is_initialized()):
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank, world, seconds):
+    """Whole-job throughput of `world` replicas that each processed
+    units_per_rank units in (at most) `seconds`."""
+    return world * units_per_rank / seconds
+
+
 def run_reference(args):
     world, rank, _ = dist_setup()
     if rank != 0:
@@ -348,12 +365,9 @@ def run_ours(args):
     kern_ms, kern_launches = ctx.profile_read()
     ctx.set_profiling(False)
     launches = ctx.launches - l0
-    if world > 1:
-        tt = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = max_over_ranks(ms, dev)
     vis_per_step = T_PER_STEP * F * N * N
-    value = world * args.steps * vis_per_step / (ms / 1e3)
+    value = job_rate(args.steps * vis_per_step, world, ms / 1e3)
     clk = clocks.summary()
 
     # ---- roofline of the contraction kernel -------------------------------
@@ -424,9 +438,9 @@ def run_ours(args):
         t0 = time.perf_counter()
         for i in range(args.steps):
             e2e_step(i)
-        e2e_s = time.perf_counter() - t0
+        e2e_s = max_over_ranks(time.perf_counter() - t0, dev)
         h2d = sum(pin[k].nbytes for k in pin) + e2t.nbytes + 8 * F
-        line["e2e"] = {"value": world * args.steps * vis_per_step / e2e_s, "unit": "vis/s",
+        line["e2e"] = {"value": job_rate(args.steps * vis_per_step, world, e2e_s), "unit": "vis/s",
                        "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(out.nbytes),
                        "api": "hera_gpu_gb300.vis_gpu_multifreq -> hv_vis_multifreq"}
 
