@@ -65,6 +65,9 @@ def parse_args():
     ap.add_argument("--serve-max-batch", type=int, default=2)
     ap.add_argument("--batch-sims", type=int, default=256,
                     help="simulations of the batched-form leg (0 = skip)")
+    ap.add_argument("--no-median", action="store_true", help="skip the median-filter leg")
+    ap.add_argument("--median-only", action="store_true",
+                    help="run only the median-filter leg and print its summary")
     ap.add_argument("--batch-only", action="store_true",
                     help="run only the batched-form leg and print its summary")
     ap.add_argument("--serve-only", action="store_true",
@@ -485,6 +488,10 @@ def run_ours(args):
     if rank == 0 and args.batch_sims > 0:
         line["batch"] = run_batch(args, local)
 
+    # ---- the 2-D median filter (hera_gpu.MedianFilter) ---------------------
+    if rank == 0 and not args.no_median:
+        line["median"] = run_median(args, local)
+
     # ---- serving: Poisson request stream, continuous batching --------------
     if rank == 0 and args.serve_requests > 0:
         line["serve"] = run_serve(args, local, pool)
@@ -496,6 +503,64 @@ def run_ours(args):
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+# the largest images and windows of the reference's median-filter tests
+# (hera_gpu/tests/test_median_filter.py): (rows, cols), (k0, k1)
+MEDIAN_CASES = [((7000, 7000), (3, 3)), ((4000, 4000), (5, 5)), ((997, 997), (9, 9)),
+                ((8013, 700), (9, 5))]
+
+
+def run_median(args, device, steps=5, warmup=3):
+    """The median filter on the reference's test shapes (uniform random
+    images): device time with the image resident (CUDA events around
+    hv_median_filter_device), end to end through MedianFilter (host arrays,
+    copies included), and scipy.signal.medfilt2d on one host core, the
+    reference's own check."""
+    import ctypes
+    import numpy as np
+    import scipy.signal as sps
+    import torch
+    from hera_gpu_gb300 import MedianFilter, _native
+    dev = torch.device("cuda", device)
+    ctx = _native.Context(device)
+    peaks, _ = load_peaks()
+    out = []
+    for (rows, cols), (k0, k1) in MEDIAN_CASES:
+        img = np.random.default_rng(0).random((rows, cols), dtype=np.float32)
+        d_in = torch.from_numpy(img).to(dev)
+        d_out = torch.empty_like(d_in)
+        stream = torch.cuda.Stream(dev)
+
+        def call():
+            ctx.check(ctx.lib.hv_median_filter_device(
+                ctx.h, ctypes.c_void_p(d_in.data_ptr()), ctypes.c_void_p(d_out.data_ptr()), 1,
+                rows, cols, k0, k1, ctypes.c_void_p(stream.cuda_stream)))
+        for _ in range(warmup):
+            call()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            call()
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        MedianFilter(input=img, kernel_size=(k0, k1), context=ctx)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            MedianFilter(input=img, kernel_size=(k0, k1), context=ctx)
+        e2e_s = (time.perf_counter() - t0) / steps
+        t0 = time.perf_counter()
+        sps.medfilt2d(img, (k0, k1))
+        cpu_s = time.perf_counter() - t0
+        px = rows * cols
+        gbs = 8.0 * px / (ms / 1e3) / 1e9
+        out.append({"image": [rows, cols], "window": [k0, k1], "ms": ms,
+                    "mpix_per_s": px / (ms / 1e3) / 1e6, "e2e_mpix_per_s": px / e2e_s / 1e6,
+                    "hbm_gbs": gbs, "hbm_frac": gbs / peaks.get("hbm_gbs", 6800.0),
+                    "cpu_scipy_mpix_per_s": px / cpu_s / 1e6})
+    return {"cases": out, "unit": "Mpixel/s", "cpu": "scipy.signal.medfilt2d, 1 host core",
+            "bytes_per_pixel": 8, "data": "uniform random float32 images"}
 
 
 def run_batch(args, device, steps=5, warmup=3):
@@ -649,6 +714,9 @@ def main():
         return 0
     if args.batch_only:
         print(json.dumps({"batch": run_batch(args, 0)}), flush=True)
+        return 0
+    if args.median_only:
+        print(json.dumps({"median": run_median(args, 0)}), flush=True)
         return 0
     return run_ours(args)
 

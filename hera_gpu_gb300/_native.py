@@ -56,6 +56,9 @@ SIGNATURES = {
     "hv_set_profiling": (_c_int, [_c_void_p, _c_int]),
     "hv_profile_read": (_c_int, [_c_void_p, ctypes.POINTER(_c_double), ctypes.POINTER(ctypes.c_uint64)]),
     "hv_set_wait_limit": (_c_int, [_c_void_p, ctypes.c_uint64, _c_int]),
+    "hv_median_filter": (_c_int, [_c_void_p, _PTR, _PTR, _c_int, _c_int, _c_int, _c_int, _c_int]),
+    "hv_median_filter_device": (_c_int, [_c_void_p, _PTR, _PTR, _c_int, _c_int, _c_int, _c_int,
+                                         _c_int, _c_void_p]),
     "hv_vis_gpu_noalloc": (_c_int, [_PTR, _c_int, _c_double, _PTR, _c_int, _PTR, _PTR, _c_int,
                                     _PTR, _c_int, _PTR, _c_void_p, ctypes.c_char_p, _c_size_t]),
     "hv_batch_create": (_c_int, [_c_void_p, ctypes.POINTER(HvSim), _c_int, ctypes.c_uint,
@@ -213,6 +216,15 @@ class Context:
         ``stall`` the next fused launches are made to time out (fault
         injection for tests of failure detection)."""
         self.check(self.lib.hv_set_wait_limit(self.h, int(wait_s * 1e9), 1 if stall else 0))
+
+    def median_filter(self, images, out, k0, k1):
+        """Median filter of the (nimg, rows, cols) float32 images into out
+        (hv_median_filter)."""
+        assert images.dtype == np.float32 and out.dtype == np.float32
+        assert images.flags.c_contiguous and out.flags.c_contiguous and images.shape == out.shape
+        n, rows, cols = images.shape
+        self.check(self.lib.hv_median_filter(self.h, _ptr(images), _ptr(out), n, rows, cols,
+                                             int(k0), int(k1)))
 
     def profile_read(self):
         """(milliseconds, launches) of the visibility-product kernels since

@@ -185,6 +185,21 @@ int hv_vis_gpu_noalloc(const void* d_antpos, int nant, double freq,
                        const void* d_bm_cube, int beam_px, void* d_vis_out,
                        void* stream, char* errbuf, size_t errlen);
 
+/* ---- 2-D median filter ---------------------------------------------------
+ * hera_gpu's MedianFilter (hera_gpu/median_filter.py:8-365): for each of
+ * nimg float32 images of rows x cols (C order, one after the other), each
+ * output pixel is the element of rank floor(k0 * k1 / 2) (0-based, ascending)
+ * of the k0 x k1 window (rows x columns) centred on it, with the image padded
+ * by zeros (median_filter.py:318; the window of pixel (r, c) starts at
+ * (r - k0/2, c - k1/2)).  For odd windows this is scipy.signal.medfilt2d.
+ * Windows whose block tile exceeds 200 KB of shared memory return
+ * HV_ERR_ARG.  The _device form takes device buffers and returns without
+ * synchronising (stream NULL = the context's stream). */
+int hv_median_filter(hv_context* ctx, const float* in, float* out, int nimg, int rows, int cols,
+                     int k0, int k1);
+int hv_median_filter_device(hv_context* ctx, const float* d_in, float* d_out, int nimg,
+                            int rows, int cols, int k0, int k1, void* stream);
+
 /* Device memory and copies ordered on the context's stream (stream-ordered
  * allocation, so freeing does not stall other streams); used by host code
  * that keeps inputs resident or serves requests.  kind: 1 host->device,

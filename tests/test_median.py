@@ -1,0 +1,81 @@
+"""The 2-D median filter (hera_gpu.MedianFilter, median_filter.py:8-365).
+
+CPU: the oracle restatement against scipy.signal.medfilt2d, the reference's
+own test oracle (hera_gpu/tests/test_median_filter.py), including 1x1
+images and windows larger than the image.  GPU: the library's kernel against
+the oracle, bit for bit (a median is a selection, no arithmetic), on the
+reference's test shapes and windows, through the drop-in MedianFilter.
+"""
+import zlib
+
+import numpy as np
+import pytest
+import scipy.signal as sps
+
+from oracle import median_filter_oracle
+
+ODD_CASES = [((1, 1), 1), ((29, 29), 1), ((29, 29), 3), ((93, 93), 3), ((1, 1), 3),
+             ((1, 1), 9), ((40, 37), 5), ((1, 73), (1, 11)), ((5, 3), (11, 1)),
+             ((2, 3), (3, 5)), ((60, 45), (9, 5)), ((31, 17), 9)]
+
+
+@pytest.mark.parametrize("shape,ks", ODD_CASES)
+def test_oracle_matches_scipy_medfilt2d(shape, ks):
+    rng = np.random.default_rng(zlib.crc32(repr((shape, ks)).encode()))
+    img = rng.random(shape).astype(np.float32)
+    k0, k1 = (ks, ks) if isinstance(ks, int) else ks
+    ref = sps.medfilt2d(img, (k0, k1))
+    np.testing.assert_array_equal(median_filter_oracle(img, k0, k1), ref)
+
+
+def test_oracle_even_window_follows_the_reference_rank():
+    # an even window (scipy refuses it) takes the rank-(k0*k1)//2 element of
+    # the window starting k//2 above/left, as the reference's kernel
+    img = np.arange(16, dtype=np.float32).reshape(4, 4)
+    out = median_filter_oracle(img, 2, 2)
+    # pixel (1, 1): padded window rows 0..1 x cols 0..1 around it = {0, 1, 4, 5}
+    assert out[1, 1] == 4.0
+
+
+gpu = pytest.mark.gpu
+REF_SHAPES = [((1, 1), 1), ((29, 29), 1), ((93, 93), 1), ((7000, 7000), 1),
+              ((1, 1), 3), ((29, 29), 3), ((93, 93), 3), ((7000, 7000), 3),
+              ((1, 1), 5), ((4000, 4000), 5), ((1, 1), 9), ((997, 997), 9),
+              ((1, 73), 1), ((5, 3), 1), ((2, 3), 3), ((8013, 700), 5),
+              ((1, 73), (1, 11)), ((5, 3), (11, 1)), ((2, 3), (3, 5)), ((8013, 700), (9, 5))]
+
+
+@gpu
+@pytest.mark.parametrize("shape,ks", REF_SHAPES)
+def test_median_filter_matches_oracle(shape, ks):
+    from hera_gpu_gb300 import MedianFilter
+    rng = np.random.default_rng(7)
+    img = rng.random(shape)
+    k0, k1 = (ks, ks) if isinstance(ks, int) else ks
+    out = MedianFilter(input=img, kernel_size=ks)
+    assert isinstance(out, list) and len(out) == 1 and out[0].shape == shape
+    ref = sps.medfilt2d(img.astype(np.float32), (k0, k1)) if max(shape) > 1000 else \
+        median_filter_oracle(img, k0, k1)
+    np.testing.assert_array_equal(out[0], ref)
+    assert np.allclose(sps.medfilt2d(img, (k0, k1)), out)   # the reference's own check
+
+
+@gpu
+def test_median_filter_list_of_images_and_negative_values():
+    from hera_gpu_gb300 import MedianFilter
+    rng = np.random.default_rng(3)
+    imgs = [rng.normal(0, 10, (50, 70)) for _ in range(5)]
+    out = MedianFilter(input=imgs, kernel_size=(3, 7))
+    assert len(out) == 5
+    for a, b in zip(imgs, out):
+        np.testing.assert_array_equal(b, median_filter_oracle(a, 3, 7))
+
+
+@gpu
+def test_median_filter_even_window_and_bad_window():
+    from hera_gpu_gb300 import MedianFilter, _native
+    img = np.random.default_rng(5).random((33, 21))
+    np.testing.assert_array_equal(MedianFilter(input=img, kernel_size=(4, 2))[0],
+                                  median_filter_oracle(img, 4, 2))
+    with pytest.raises(_native.HeraVisError):
+        MedianFilter(input=img, kernel_size=(301, 301))   # its tile exceeds shared memory
