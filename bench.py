@@ -68,6 +68,9 @@ def parse_args():
     ap.add_argument("--no-median", action="store_true", help="skip the median-filter leg")
     ap.add_argument("--median-only", action="store_true",
                     help="run only the median-filter leg and print its summary")
+    ap.add_argument("--no-omnical", action="store_true", help="skip the omnical leg")
+    ap.add_argument("--omnical-only", action="store_true",
+                    help="run only the omnical leg and print its summary")
     ap.add_argument("--batch-only", action="store_true",
                     help="run only the batched-form leg and print its summary")
     ap.add_argument("--serve-only", action="store_true",
@@ -492,6 +495,10 @@ def run_ours(args):
     if rank == 0 and not args.no_median:
         line["median"] = run_median(args, local)
 
+    # ---- Omnical redundant calibration (hera_gpu.redcal.omnical) -----------
+    if rank == 0 and not args.no_omnical:
+        line["omnical"] = run_omnical(args, local)
+
     # ---- serving: Poisson request stream, continuous batching --------------
     if rank == 0 and args.serve_requests > 0:
         line["serve"] = run_serve(args, local, pool)
@@ -561,6 +568,86 @@ def run_median(args, device, steps=5, warmup=3):
                     "cpu_scipy_mpix_per_s": px / cpu_s / 1e6})
     return {"cases": out, "unit": "Mpixel/s", "cpu": "scipy.signal.medfilt2d, 1 host core",
             "bytes_per_pixel": 8, "data": "uniform random float32 images"}
+
+
+# the configurations of the reference's own omnical timings
+# (hera_gpu/redcal.py:438-458: 2000 problems, Quadro T2000, the shipped
+# chunk_size = nthreads // 16): (nants, precision, seconds there)
+OMNICAL_CASES = [(54, 2, 1.5), (126, 2, 5.2), (180, 2, 9.9), (180, 1, 7.3)]
+OMNICAL_NDATA = 2000
+
+
+def run_omnical(args, device, steps=3, warmup=3, cpu_sample=8):
+    """Omnical with the reference's defaults (conv_crit 1e-10, maxiter 50,
+    check_every 4, check_after 1, gain 0.3) on 2000 problems of a hex
+    redundant array of nants antennas (synthetic: gains 1 + 5% scatter, 1%
+    noise, start 2% off).  Device time with the inputs resident (CUDA events
+    around the reset of the starting point and hv_omnical_device), end to
+    end through the drop-in omnical (host arrays, copies included), and the
+    oracle on a sample of problems on one host core, extrapolated."""
+    import ctypes
+    import numpy as np
+    import torch
+    from hera_gpu_gb300 import _native, omnical, synth
+    from oracle import omnical_oracle
+    dev = torch.device("cuda", device)
+    ctx = _native.Context(device)
+    out = []
+    for nants, precision, ref_s in OMNICAL_CASES:
+        ggu, nubls = synth.hex_redundant_layout(nants)
+        nbls = len(ggu)
+        g0, u0, d, w = synth.redundant_data(ggu, nubls, OMNICAL_NDATA, seed=nants, noise=0.01)
+        ct, rt = (np.complex64, np.float32) if precision == 1 else (np.complex128, np.float64)
+        g0, u0, d, w = g0.astype(ct), u0.astype(ct), d.astype(ct), w.astype(rt)
+        t = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+             for k, v in (("g0", g0), ("u0", u0), ("d", d), ("w", w))}
+        tg, tu = torch.empty_like(t["g0"]), torch.empty_like(t["u0"])
+        tc, tv = torch.empty(OMNICAL_NDATA, dtype=t["w"].dtype, device=dev), \
+            torch.empty(OMNICAL_NDATA, dtype=t["w"].dtype, device=dev)
+        ti = torch.empty(OMNICAL_NDATA, dtype=torch.int32, device=dev)
+        stream = torch.cuda.Stream(dev)
+        vp = lambda x: ctypes.c_void_p(x.data_ptr())
+
+        def call():
+            with torch.cuda.stream(stream):
+                tg.copy_(t["g0"])
+                tu.copy_(t["u0"])
+            ctx.check(ctx.lib.hv_omnical_device(
+                ctx.h, precision, ggu.ctypes.data_as(ctypes.c_void_p), nbls, vp(tg), nants,
+                vp(tu), nubls, vp(t["d"]), vp(t["w"]), OMNICAL_NDATA, 1e-10, 50, 4, 1, 0.3,
+                vp(tc), vp(ti), vp(tv), ctypes.c_void_p(stream.cuda_stream)))
+        for _ in range(warmup):
+            call()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            call()
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        iters = ti.cpu().numpy()
+        omnical(ggu, g0, u0, d, w, precision=precision, context=ctx)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            res = omnical(ggu, g0, u0, d, w, precision=precision, context=ctx)
+        e2e_s = (time.perf_counter() - t0) / steps
+        t0 = time.perf_counter()
+        ref = omnical_oracle(ggu, g0[:cpu_sample], u0[:cpu_sample], d[:cpu_sample],
+                             w[:cpu_sample], precision=precision)
+        cpu_s = (time.perf_counter() - t0) / cpu_sample * OMNICAL_NDATA
+        scale = float(np.abs(ref["gains"]).max())
+        out.append({
+            "nants": nants, "nbls": nbls, "nubls": nubls, "precision": precision,
+            "problems": OMNICAL_NDATA, "ms": ms, "problems_per_s": OMNICAL_NDATA / (ms / 1e3),
+            "e2e_s": e2e_s, "mean_iters": float(iters.mean()),
+            "reference_published_s": ref_s,
+            "cpu_oracle_s_extrapolated": cpu_s,
+            "max_gain_diff_vs_oracle": float(np.abs(res["gains"][:cpu_sample] - ref["gains"]).max()
+                                             / scale),
+            "iters_equal_vs_oracle": float((res["iters"][:cpu_sample] == ref["iters"]).mean())})
+    return {"cases": out, "data": "synthetic hex redundant arrays, 1% noise",
+            "reference_published": "hera_gpu/redcal.py:438-458, Quadro T2000, other hardware",
+            "cpu": f"oracle (numpy, 1 process) on {cpu_sample} problems, extrapolated"}
 
 
 def run_batch(args, device, steps=5, warmup=3):
@@ -717,6 +804,9 @@ def main():
         return 0
     if args.median_only:
         print(json.dumps({"median": run_median(args, 0)}), flush=True)
+        return 0
+    if args.omnical_only:
+        print(json.dumps({"omnical": run_omnical(args, 0)}), flush=True)
         return 0
     return run_ours(args)
 

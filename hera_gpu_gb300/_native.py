@@ -59,6 +59,12 @@ SIGNATURES = {
     "hv_median_filter": (_c_int, [_c_void_p, _PTR, _PTR, _c_int, _c_int, _c_int, _c_int, _c_int]),
     "hv_median_filter_device": (_c_int, [_c_void_p, _PTR, _PTR, _c_int, _c_int, _c_int, _c_int,
                                          _c_int, _c_void_p]),
+    "hv_omnical": (_c_int, [_c_void_p, _c_int, _PTR, _c_int, _PTR, _c_int, _PTR, _c_int, _PTR,
+                            _PTR, _c_int, _c_double, _c_int, _c_int, _c_int, _c_double, _PTR,
+                            _PTR, _PTR]),
+    "hv_omnical_device": (_c_int, [_c_void_p, _c_int, _PTR, _c_int, _PTR, _c_int, _PTR, _c_int,
+                                   _PTR, _PTR, _c_int, _c_double, _c_int, _c_int, _c_int,
+                                   _c_double, _PTR, _PTR, _PTR, _c_void_p]),
     "hv_vis_gpu_noalloc": (_c_int, [_PTR, _c_int, _c_double, _PTR, _c_int, _PTR, _PTR, _c_int,
                                     _PTR, _c_int, _PTR, _c_void_p, ctypes.c_char_p, _c_size_t]),
     "hv_batch_create": (_c_int, [_c_void_p, ctypes.POINTER(HvSim), _c_int, ctypes.c_uint,
@@ -225,6 +231,21 @@ class Context:
         n, rows, cols = images.shape
         self.check(self.lib.hv_median_filter(self.h, _ptr(images), _ptr(out), n, rows, cols,
                                              int(k0), int(k1)))
+
+    def omnical(self, precision, ggu, gains, ubls, data, wgts, conv_crit, maxiter, check_every,
+                check_after, gain, chisq, iters, conv):
+        """Omnical on host arrays (hv_omnical): gains and ubls are updated in
+        place; chisq, iters and conv are filled."""
+        rt, ct = (np.float32, np.complex64) if precision == 1 else (np.float64, np.complex128)
+        for a, t in ((gains, ct), (ubls, ct), (data, ct), (wgts, rt), (chisq, rt), (conv, rt),
+                     (iters, np.uint32), (ggu, np.uint32)):
+            assert a.dtype == t and a.flags.c_contiguous
+        ndata, nants = gains.shape
+        self.check(self.lib.hv_omnical(self.h, int(precision), _ptr(ggu), ggu.shape[0],
+                                       _ptr(gains), nants, _ptr(ubls), ubls.shape[1], _ptr(data),
+                                       _ptr(wgts), ndata, float(conv_crit), int(maxiter),
+                                       int(check_every), int(check_after), float(gain),
+                                       _ptr(chisq), _ptr(iters), _ptr(conv)))
 
     def profile_read(self):
         """(milliseconds, launches) of the visibility-product kernels since

@@ -13,6 +13,9 @@ Each generator returns plain numpy arrays in the argument order of
 * ``bm_cubes`` (nfreq, nant, P, P) beam power on the (l, m) grid
   ``linspace(-1, 1, P)`` (axis order ``[ant, m(y), l(x)]`` as the reference's
   ``bm_cube``).
+
+and, for the Omnical solver, redundant array layouts (``ggu_indices``) and
+seeded redundant-calibration problems (``redundant_data``).
 """
 from __future__ import annotations
 
@@ -177,3 +180,59 @@ def make_sim(spec, dtype=np.float32):
         bm[i] = airy_beams(spec["nant"], spec["P"], f, dish)
     sim["bm_cubes"] = bm
     return sim
+
+
+# ---- redundant-calibration problems (omnical) ------------------------------
+
+def linear_redundant_layout(nants):
+    """Every pair i > j of a linear array of nants evenly spaced antennas,
+    unique baseline i - j - 1 (the layout of hera_gpu's omnical tests,
+    test_redcal.py:62-63): (ggu_indices (nbls, 3) uint32, nubls)."""
+    ggu = np.array([(i, j, i - j - 1) for i in range(nants) for j in range(i)],
+                   dtype=np.uint32).reshape(-1, 3)
+    return ggu, max(nants - 1, 0)
+
+
+def hex_redundant_layout(nants):
+    """A 2-D redundant array: the nants points of a triangular lattice
+    nearest its centre; every pair oriented so its separation vector is
+    canonical (lexicographically positive), unique baselines numbered by
+    distinct separation in pair order: (ggu_indices (nbls, 3) uint32, nubls)."""
+    r = int(np.ceil(np.sqrt(nants))) + 2
+    pts = [(a, b) for a in range(-r, r + 1) for b in range(-r, r + 1)]
+    pts.sort(key=lambda p: (p[0] ** 2 + p[1] ** 2 + p[0] * p[1], p))
+    pts = pts[:nants]
+    ubl, out = {}, []
+    for i in range(nants):
+        for j in range(i):
+            v = (pts[i][0] - pts[j][0], pts[i][1] - pts[j][1])
+            a, b = i, j
+            if v < (0, 0):
+                v, a, b = (-v[0], -v[1]), j, i
+            out.append((a, b, ubl.setdefault(v, len(ubl))))
+    return np.array(out, dtype=np.uint32).reshape(-1, 3), len(ubl)
+
+
+def redundant_data(ggu, nubls, ndata, seed=0, noise=0.0, scatter=0.05, perturb=0.02):
+    """ndata redundant problems on the layout ggu: true gains 1 + scatter
+    (complex normal), unit-variance complex unique baselines, data with
+    complex noise of rms `noise` per component, unit weights, and a starting
+    point -- gains perturbed by `perturb`, unique baselines averaged over
+    their group from those gains.  Returns (gains0, ubls0, data, wgts), all
+    complex128 / float64."""
+    rng = np.random.default_rng(seed)
+    nants = int(ggu[:, :2].max()) + 1 if len(ggu) else 0
+    gi, gj, uk = (ggu[:, c].astype(np.int64) for c in range(3))
+    g = 1 + scatter * (rng.normal(size=(ndata, nants)) + 1j * rng.normal(size=(ndata, nants)))
+    u = rng.normal(size=(ndata, nubls)) + 1j * rng.normal(size=(ndata, nubls))
+    d = g[:, gi] * np.conj(g[:, gj]) * u[:, uk]
+    if noise:
+        d = d + noise * (rng.normal(size=d.shape) + 1j * rng.normal(size=d.shape))
+    w = np.ones(d.shape)
+    g0 = g * (1 + perturb * (rng.normal(size=g.shape) + 1j * rng.normal(size=g.shape)))
+    r = d / (g0[:, gi] * np.conj(g0[:, gj]))
+    cnt = np.maximum(np.bincount(uk, minlength=nubls), 1)
+    u0 = np.zeros((ndata, nubls), complex)
+    for k in range(nubls):
+        u0[:, k] = r[:, uk == k].sum(axis=1)
+    return g0, u0 / cnt, d, w

@@ -200,6 +200,34 @@ int hv_median_filter(hv_context* ctx, const float* in, float* out, int nimg, int
 int hv_median_filter_device(hv_context* ctx, const float* d_in, float* d_out, int nimg,
                             int rows, int cols, int k0, int k1, void* stream);
 
+/* ---- Omnical redundant calibration --------------------------------------
+ * hera_gpu's omnical (hera_gpu/redcal.py:358-743): for each of ndata
+ * independent problems p, iterate the Omnical solution of
+ *   data[p][b] = gains[p][i_b] * conj(gains[p][j_b]) * ubls[p][k_b]
+ * with (i_b, j_b, k_b) = ggu[3 b .. 3 b + 2] (a HOST array of nbls uint32
+ * triples, redcal.py:392-393,423), as the reference's kernels do
+ * (redcal.py:70-354): weights every check_every iterations, a step of
+ * fraction `gain` toward the new estimate each iteration, and a
+ * convergence / chi^2 check every check_every iterations from check_after on
+ * and at maxiter (redcal.py:587-702).  precision 1: complex64 gains, ubls
+ * and data, float32 wgts, chisq and conv; precision 2: complex128 / float64.
+ * gains (ndata x nants) and ubls (ndata x nubls) are overwritten with the
+ * solutions; chisq, iters (the last accepted iteration, 0 if none) and conv
+ * (the last relative change) get one value per problem (redcal.py:742).
+ * check_every must be > 1 (redcal.py:402), nants <= 65535; a triple out of
+ * range returns HV_ERR_ARG.  The _device form takes device buffers (ggu
+ * still on the host) and returns without synchronising (stream NULL = the
+ * context's stream). */
+int hv_omnical(hv_context* ctx, int precision, const uint32_t* ggu, int nbls, void* gains,
+               int nants, void* ubls, int nubls, const void* data, const void* wgts, int ndata,
+               double conv_crit, int maxiter, int check_every, int check_after, double gain,
+               void* chisq, uint32_t* iters, void* conv);
+int hv_omnical_device(hv_context* ctx, int precision, const uint32_t* ggu, int nbls,
+                      void* d_gains, int nants, void* d_ubls, int nubls, const void* d_data,
+                      const void* d_wgts, int ndata, double conv_crit, int maxiter,
+                      int check_every, int check_after, double gain, void* d_chisq,
+                      uint32_t* d_iters, void* d_conv, void* stream);
+
 /* Device memory and copies ordered on the context's stream (stream-ordered
  * allocation, so freeing does not stall other streams); used by host code
  * that keeps inputs resident or serves requests.  kind: 1 host->device,
