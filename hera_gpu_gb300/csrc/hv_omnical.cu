@@ -20,8 +20,9 @@
 // a time and scatters with global atomics.  Here one launch solves every
 // problem: one CTA per problem (a persistent grid that takes problems from
 // a counter), every iteration inside the kernel, the solution and the
-// per-baseline arrays in shared memory, the model recomputed from the
-// solution where it is needed.  The sums over each antenna's and each unique
+// per-baseline values in shared memory (a panel of baselines at a time when
+// they do not all fit), the model recomputed from the solution where it is
+// needed.  The sums over each antenna's and each unique
 // baseline's baselines are gathers over a fixed incidence list (CSR), each
 // segment summed by a fixed group of lanes in a fixed order, so the result
 // does not depend on scheduling and repeats bit for bit.
@@ -52,17 +53,22 @@ constexpr int kOmMaxThreads = 512;
 #define OM_MINB 2  // CTAs of 512 threads an SM: 64 registers a thread
 #endif
 constexpr int kOmSmemLimit = 226 * 1024;  // dynamic shared memory, below the 227 KB per CTA
-
-// Which per-baseline arrays live in shared memory (otherwise: d in a per-CTA
-// global workspace, data and wgts read from the inputs).
-enum : int { kOmSmemD = 1, kOmSmemData = 2 };
+constexpr int kOmThreadsPerSm = 1024 * (OM_MINB > 2 ? 2 : OM_MINB) / 2;  // register limit
+#ifndef OM_GK_D
+#define OM_GK_D 16  // float64 gathers: entries a lane at least
+#endif
+#ifndef OM_WANT_F
+#define OM_WANT_F 2  // CTAs of 512 threads an SM the panels are sized for
+#define OM_WANT_D 2
+#endif
 
 template <typename R>
 struct OmParams {
   int ndata, nants, nubls, nbls;
+  int panel, npanels;     // baselines per panel (the last may be shorter), panels
   const uint2* bl;        // [nbls] (i | j << 16, k)
-  const int* seg_off;     // [nants + nubls + 1]: antennas, then unique baselines
-  const uint32_t* seg_ent;// baseline | (conjugate << 31)
+  const int* seg_off;     // [npanels][nants + nubls + 1] into seg_ent
+  const uint32_t* seg_ent;// baseline within its panel | (conjugate << 31)
   const typename Cx<R>::T* data;  // [ndata][nbls]
   const R* wgts;                  // [ndata][nbls]
   typename Cx<R>::T* gains;       // [ndata][nants], in/out
@@ -74,8 +80,6 @@ struct OmParams {
   float gstep;
   int maxiter, check_every, check_after;
   int group;       // lanes per segment in the gathers (1, 2, 4, 8, 16 or 32)
-  char* ws;        // per-CTA workspace for the arrays not in shared memory
-  size_t ws_stride;
   int* counter;    // next problem
 };
 
@@ -96,10 +100,10 @@ __device__ __forceinline__ auto mag2(C a) -> decltype(a.x) {
   return a.x * a.x + a.y * a.y;
 }
 
-// g[i] conj(g[j]) u[k] (gen_dmdl, redcal.py:70-94)
+// g[i] conj(g[j]) u[k] (gen_dmdl, redcal.py:70-94); sol = g | u
 template <typename C>
-__device__ __forceinline__ C model(const C* g, const C* u, uint2 e) {
-  return cmul(cmul(g[e.x & 0xffffu], conjc(g[e.x >> 16])), u[e.y]);
+__device__ __forceinline__ C model(const C* sol, int nants, uint2 e) {
+  return cmul(cmul(sol[e.x & 0xffffu], conjc(sol[e.x >> 16])), sol[nants + e.y]);
 }
 
 // Sum of three values over the block, in a fixed order; every thread gets
@@ -190,7 +194,7 @@ template <typename R> struct Unroll {
 // sum_b |data_b - model_b|^2 w_b over this thread's baselines (calc_chisq,
 // redcal.py:97-114)
 template <typename R, typename C>
-__device__ __forceinline__ R chisq_part(const C* g, const C* u, const uint2* __restrict__ bl,
+__device__ __forceinline__ R chisq_part(const C* sol, int nants, const uint2* __restrict__ bl,
                                         const C* data, const R* wgt, int nbls) {
   constexpr int U = Unroll<R>::n;
   R acc = 0;
@@ -210,7 +214,7 @@ __device__ __forceinline__ R chisq_part(const C* g, const C* u, const uint2* __r
 #pragma unroll
     for (int q = 0; q < U; ++q) {
       if (b0 + q * blockDim.x < nbls) {
-        const C m = model(g, u, e[q]);
+        const C m = model(sol, nants, e[q]);
         const R dx = x[q].x - m.x, dy = x[q].y - m.y;
         acc += (dx * dx + dy * dy) * w[q];
       }
@@ -219,42 +223,42 @@ __device__ __forceinline__ R chisq_part(const C* g, const C* u, const uint2* __r
   return acc;
 }
 
-// One CTA per problem.  Shared memory: g, gn (nants) and u, un (nubls)
-// complex; gw, mg0, ra (nants) and uw, mu0, ru (nubls) real; reduction
-// scratch; then d (complex, per baseline; also the weights dwgts on the
-// iterations that form them) and data (complex) and w, if they fit
-// (OmParams::in_smem), else d in the per-CTA workspace and data and w read
-// from the inputs.
+// One CTA per problem.  Shared memory, per segment (antennas, then unique
+// baselines): the solution and the stepped solution (complex, swapped after
+// each accepted step; the stepped one also holds the partial sums of the
+// panels before the last), the weights gwgt | uwgt, the magnitudes when they
+// were formed and their ratios to the current ones; reduction scratch; d for
+// one panel of baselines (complex; also the weights dwgts while they are
+// formed); with one panel, data and w too (kDataShared), else they are read
+// from global memory (the L2 keeps a problem's rows across its iterations).
+//
+// The baselines are taken a panel at a time: the per-baseline values of a
+// panel, then its gathers, the panel sums added in panel order.  Panels keep
+// the shared memory of a CTA small enough for two CTAs an SM.
 //
 // dwgts_b / |dmdl_b|^2 of calc_gu_buf (redcal.py:219) is
 // w_b |m0_b|^2 / |m_b|^2 with m0 the model when the weights were formed;
 // |m_b|^2 = |g_i|^2 |g_j|^2 |u_k|^2, so the factor is taken as
 // w_b ra_i ra_j ru_k with ra = |g0|^2 / |g|^2 per antenna and ru per unique
 // baseline: nants + nubls divisions an iteration instead of nbls.
-template <typename R, int kLayout>
+template <typename R, bool kDataShared>
 __global__ void __launch_bounds__(kOmMaxThreads, OM_MINB) omnical_kernel(const OmParams<R> p) {
   using C = typename Cx<R>::T;
   constexpr int U = Unroll<R>::n;
-  constexpr bool kDShared = (kLayout & kOmSmemD) != 0, kDataShared = (kLayout & kOmSmemData) != 0;
   extern __shared__ __align__(16) unsigned char smem[];
   const int nants = p.nants, nubls = p.nubls, nbls = p.nbls, nseg = nants + nubls;
-  C* gA = reinterpret_cast<C*>(smem);
-  C* gB = gA + nants;
-  C* uA = gB + nants;
-  C* uB = uA + nubls;
-  R* gw = reinterpret_cast<R*>(uB + nubls);  // gw | uw
-  R* uw = gw + nants;
-  R* mg0 = uw + nubls;                        // mg0 | mu0
-  R* mu0 = mg0 + nants;
-  R* ra = mu0 + nubls;                        // ra | ru
-  R* ru = ra + nants;
-  R* red = ru + nubls;  // 96 values
+  const int PB = p.panel, np = p.npanels;
+  C* const solA = reinterpret_cast<C*>(smem);
+  C* const solB = solA + nseg;
+  R* const gw = reinterpret_cast<R*>(solB + nseg);  // gwgt | uwgt
+  R* const mg0 = gw + nseg;                         // |g0|^2 | |u0|^2
+  R* const ra = mg0 + nseg;                         // ratios
+  R* const red = ra + nseg;                         // 96 values
   unsigned char* next = reinterpret_cast<unsigned char*>(red + 96);
   next = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(next) + 15) & ~uintptr_t(15));
-  C* const d = kDShared ? reinterpret_cast<C*>(next)
-                        : reinterpret_cast<C*>(p.ws + (size_t)blockIdx.x * p.ws_stride);
+  C* const d = reinterpret_cast<C*>(next);
   R* const dw = reinterpret_cast<R*>(d);
-  C* const sdata = reinterpret_cast<C*>(next + sizeof(C) * (size_t)nbls);
+  C* const sdata = d + PB;
   R* const sw = reinterpret_cast<R*>(sdata + nbls);
   __shared__ int s_prob;
 
@@ -271,8 +275,8 @@ __global__ void __launch_bounds__(kOmMaxThreads, OM_MINB) omnical_kernel(const O
     if (prob >= p.ndata) return;
     const C* const gdata = p.data + (size_t)prob * nbls;
     const R* const gwgt = p.wgts + (size_t)prob * nbls;
-    for (int a = tid; a < nants; a += nt) gA[a] = p.gains[(size_t)prob * nants + a];
-    for (int k = tid; k < nubls; k += nt) uA[k] = p.ubls[(size_t)prob * nubls + k];
+    for (int a = tid; a < nants; a += nt) solA[a] = p.gains[(size_t)prob * nants + a];
+    for (int k = tid; k < nubls; k += nt) solA[nants + k] = p.ubls[(size_t)prob * nubls + k];
     if (kDataShared) {
       for (int b = tid; b < nbls; b += nt) {
         sdata[b] = __ldg(gdata + b);
@@ -282,10 +286,10 @@ __global__ void __launch_bounds__(kOmMaxThreads, OM_MINB) omnical_kernel(const O
     const C* const data = kDataShared ? sdata : gdata;
     const R* const wgt = kDataShared ? sw : gwgt;
     __syncthreads();
-    C *g = gA, *gn = gB, *u = uA, *un = uB;
+    C *sol = solA, *nsol = solB;
 
     // chi^2 of the starting solution (redcal.py:566-577)
-    R chisq = chisq_part(g, u, bl, data, wgt, nbls), z1 = 0, z2 = 0;
+    R chisq = chisq_part(sol, nants, bl, data, wgt, nbls), z1 = 0, z2 = 0;
     block_sum3(chisq, z1, z2, red);
     R conv = 0;
     uint32_t iters = 0;
@@ -294,88 +298,86 @@ __global__ void __launch_bounds__(kOmMaxThreads, OM_MINB) omnical_kernel(const O
       if (it % p.check_every == 1) {
         // weights from the current model (calc_dwgts, calc_gu_wgt)
         for (int s = tid; s < nseg; s += nt) {
-          const C x = s < nants ? g[s] : u[s - nants];
-          mg0[s] = mag2(x);
+          mg0[s] = mag2(sol[s]);
           ra[s] = 1;
         }
-        for (int b0 = tid; b0 < nbls; b0 += U * nt) {
+        for (int pn = 0; pn < np; ++pn) {
+          const int b0 = pn * PB, nb = min(PB, nbls - b0);
+          for (int b = tid; b < nb; b += nt) dw[b] = mag2(model(sol, nants, bl[b0 + b])) * wgt[b0 + b];
+          __syncthreads();
+          seg_gather<Unroll<R>::gather, RealV<R>>(
+              p.seg_off + (size_t)pn * (nseg + 1), p.seg_ent, nseg, p.group,
+              [&](uint32_t e) { return RealV<R>{dw[e & 0x7fffffffu]}; },
+              [&](int s, RealV<R> v) { gw[s] = pn ? gw[s] + v.v : v.v; });
+          __syncthreads();  // dw is overwritten below
+        }
+      } else {
+        for (int s = tid; s < nseg; s += nt) ra[s] = mg0[s] / mag2(sol[s]);
+        __syncthreads();
+      }
+      // d_b = data_b conj(m_b) dwgts_b / |m_b|^2 (calc_gu_buf), summed per
+      // antenna and unique baseline, then the step (update_gains/_ubls)
+      for (int pn = 0; pn < np; ++pn) {
+        const int b0 = pn * PB, nb = min(PB, nbls - b0);
+        for (int c0 = tid; c0 < nb; c0 += U * nt) {
           uint2 e[U];
+          C x[U];
           R w[U];
 #pragma unroll
           for (int q = 0; q < U; ++q)
-            if (b0 + q * nt < nbls) {
-              e[q] = bl[b0 + q * nt];
-              w[q] = wgt[b0 + q * nt];
+            if (c0 + q * nt < nb) {
+              e[q] = bl[b0 + c0 + q * nt];
+              x[q] = data[b0 + c0 + q * nt];
+              w[q] = wgt[b0 + c0 + q * nt];
             }
 #pragma unroll
           for (int q = 0; q < U; ++q)
-            if (b0 + q * nt < nbls) dw[b0 + q * nt] = mag2(model(g, u, e[q])) * w[q];
+            if (c0 + q * nt < nb) {
+              const int i = e[q].x & 0xffffu, j = e[q].x >> 16;
+              const C m = model(sol, nants, e[q]);
+              const R t = w[q] * ra[i] * ra[j] * ra[nants + e[q].y];
+              C z = cmul(x[q], conjc(m));
+              z.x *= t;
+              z.y *= t;
+              d[c0 + q * nt] = z;
+            }
         }
         __syncthreads();
-        seg_gather<Unroll<R>::gather, RealV<R>>(
-            p.seg_off, p.seg_ent, nseg, p.group,
-            [&](uint32_t e) { return RealV<R>{dw[e & 0x7fffffffu]}; },
-            [&](int s, RealV<R> v) { gw[s] = v.v; });
-        __syncthreads();  // dw is overwritten by d below
-      } else {
-        for (int s = tid; s < nseg; s += nt) {
-          const C x = s < nants ? g[s] : u[s - nants];
-          ra[s] = mg0[s] / mag2(x);
-        }
+        const bool last = pn == np - 1;
+        seg_gather<Unroll<R>::gather, CplxV<R>>(
+            p.seg_off + (size_t)pn * (nseg + 1), p.seg_ent, nseg, p.group,
+            [&](uint32_t e) {
+              const C z = d[e & 0x7fffffffu];
+              return CplxV<R>{z.x, (e >> 31) ? -z.y : z.y};
+            },
+            [&](int s, CplxV<R> v) {
+              if (pn) {
+                v.x = nsol[s].x + v.x;
+                v.y = nsol[s].y + v.y;
+              }
+              C f;
+              if (!last) {
+                f.x = v.x;
+                f.y = v.y;
+                nsol[s] = f;  // partial sum
+                return;
+              }
+              f.x = one_m + gs * v.x / gw[s];
+              f.y = gs * v.y / gw[s];
+              nsol[s] = cmul(sol[s], f);
+            });
         __syncthreads();
       }
-      // d_b = data_b conj(m_b) dwgts_b / |m_b|^2 (calc_gu_buf)
-      for (int b0 = tid; b0 < nbls; b0 += U * nt) {
-        uint2 e[U];
-        C x[U];
-        R w[U];
-#pragma unroll
-        for (int q = 0; q < U; ++q)
-          if (b0 + q * nt < nbls) {
-            e[q] = bl[b0 + q * nt];
-            x[q] = data[b0 + q * nt];
-            w[q] = wgt[b0 + q * nt];
-          }
-#pragma unroll
-        for (int q = 0; q < U; ++q)
-          if (b0 + q * nt < nbls) {
-            const int i = e[q].x & 0xffffu, j = e[q].x >> 16;
-            const C m = model(g, u, e[q]);
-            const R t = w[q] * ra[i] * ra[j] * ru[e[q].y];
-            C z = cmul(x[q], conjc(m));
-            z.x *= t;
-            z.y *= t;
-            d[b0 + q * nt] = z;
-          }
-      }
-      __syncthreads();
-      // the stepped solution (update_gains / update_ubls)
-      seg_gather<Unroll<R>::gather, CplxV<R>>(
-          p.seg_off, p.seg_ent, nseg, p.group,
-          [&](uint32_t e) {
-            const C z = d[e & 0x7fffffffu];
-            return CplxV<R>{z.x, (e >> 31) ? -z.y : z.y};
-          },
-          [&](int s, CplxV<R> v) {
-            C f;
-            f.x = one_m + gs * v.x / gw[s];
-            f.y = gs * v.y / gw[s];
-            if (s < nants) gn[s] = cmul(g[s], f);
-            else un[s - nants] = cmul(u[s - nants], f);
-          });
-      __syncthreads();
       const bool check = !(it < p.maxiter && (it < p.check_after || it % p.check_every != 0));
       if (!check) {
-        C* t = g; g = gn; gn = t;
-        t = u; u = un; un = t;
+        C* t = sol; sol = nsol; nsol = t;
         continue;
       }
       // convergence and chi^2 of the stepped solution (calc_conv,
       // calc_chisq, update_active)
-      R nchisq = chisq_part(gn, un, bl, data, wgt, nbls), csum = 0, cwgt = 0;
+      R nchisq = chisq_part(nsol, nants, bl, data, wgt, nbls), csum = 0, cwgt = 0;
       for (int s = tid; s < nseg; s += nt) {
-        const C x = s < nants ? gn[s] : un[s - nants];
-        const C y = s < nants ? g[s] : u[s - nants];
+        const C x = nsol[s], y = sol[s];
         const R dx = x.x - y.x, dy = x.y - y.y;
         csum += dx * dx + dy * dy;
         cwgt += mag2(x);
@@ -385,12 +387,11 @@ __global__ void __launch_bounds__(kOmMaxThreads, OM_MINB) omnical_kernel(const O
       if (conv < p.conv_crit || nchisq > chisq) break;
       chisq = nchisq;
       iters = (uint32_t)it;
-      C* t = g; g = gn; gn = t;
-      t = u; u = un; un = t;
+      C* t = sol; sol = nsol; nsol = t;
     }
     __syncthreads();
-    for (int a = tid; a < nants; a += nt) p.gains[(size_t)prob * nants + a] = g[a];
-    for (int k = tid; k < nubls; k += nt) p.ubls[(size_t)prob * nubls + k] = u[k];
+    for (int a = tid; a < nants; a += nt) p.gains[(size_t)prob * nants + a] = sol[a];
+    for (int k = tid; k < nubls; k += nt) p.ubls[(size_t)prob * nubls + k] = sol[nants + k];
     if (tid == 0) {
       p.chisq[prob] = chisq;
       p.conv[prob] = conv;
@@ -400,55 +401,55 @@ __global__ void __launch_bounds__(kOmMaxThreads, OM_MINB) omnical_kernel(const O
 }
 
 struct Plan {
-  int threads = 64, group = 1, in_smem = 0, blocks_per_sm = 1;
-  size_t smem = 0, ws_stride = 0;
+  int threads = 64, group = 1, blocks_per_sm = 1, panel = 0, npanels = 1;
+  bool data_shared = false;
+  size_t smem = 0;
 };
 
+// Launch shape: threads = about half the baselines (64 .. 512); everything
+// in shared memory when that leaves 16 warps an SM, else panels of
+// baselines sized for two CTAs (or the thread limit) an SM.
 template <typename R>
-Plan make_plan(int nants, int nubls, int nbls, int nsm_threads_cap) {
+int make_plan(int nants, int nubls, int nbls, Plan* out) {
   using C = typename Cx<R>::T;
   Plan pl;
-  int t = ((nbls / 2 + 31) / 32) * 32;
+  const int t = ((nbls / 2 + 31) / 32) * 32;
   pl.threads = std::max(64, std::min(kOmMaxThreads, t));
-  const size_t fixed =
-      (2 * sizeof(C) + 3 * sizeof(R)) * (size_t)(nants + nubls) + 96 * sizeof(R) + 16;
-  const size_t pd = sizeof(C) * (size_t)nbls;
-  const size_t pdata = (sizeof(C) + sizeof(R)) * (size_t)nbls;
-  const int options[3] = {kOmSmemD | kOmSmemData, kOmSmemD, 0};
-  auto bytes = [&](int f) {
-    return fixed + ((f & kOmSmemD) ? pd : 0) + ((f & kOmSmemData) ? pdata : 0);
-  };
+  const size_t nseg = (size_t)nants + nubls;
+  const size_t fixed = (2 * sizeof(C) + 3 * sizeof(R)) * nseg + 96 * sizeof(R) + 16;
   auto per_sm = [&](size_t s) {
-    return std::min(32, std::min(nsm_threads_cap / pl.threads, (int)((228 * 1024) / (s + 1024))));
+    return std::min(32, std::min(kOmThreadsPerSm / pl.threads, (int)((228 * 1024) / (s + 1024))));
   };
-  // the first layout that keeps at least 16 warps per SM, else the one
-  // with the most
-  int best = -1, best_threads = -1;
-  for (int i = 0; i < 3; ++i) {
-    const size_t s = bytes(options[i]);
-    if (s > (size_t)kOmSmemLimit) continue;
-    const int bps = per_sm(s);
-    if (bps < 1) continue;
-    if (bps * pl.threads >= 512) {
-      best = i;
-      break;
-    }
-    if (bps * pl.threads > best_threads) {
-      best = i;
-      best_threads = bps * pl.threads;
-    }
+  const size_t all = fixed + (2 * sizeof(C) + sizeof(R)) * (size_t)nbls;
+  if (all <= (size_t)kOmSmemLimit && per_sm(all) * pl.threads >= 512) {
+    pl.data_shared = true;
+    pl.panel = std::max(nbls, 1);
+    pl.npanels = 1;
+    pl.smem = all;
+  } else {
+    const int want = std::max(1, (sizeof(R) == 4 ? OM_WANT_F : OM_WANT_D) * 512 / pl.threads);
+    const size_t target = std::min((size_t)kOmSmemLimit, (size_t)(228 * 1024) / want - 1024);
+    if (fixed + 32 * sizeof(C) > target) return HV_ERR_ARG;
+    const size_t pb = std::min((size_t)std::max(nbls, 1), (target - fixed) / sizeof(C));
+    pl.npanels = (int)((nbls + pb - 1) / pb);
+    pl.npanels = std::max(pl.npanels, 1);
+    pl.panel = (nbls + pl.npanels - 1) / pl.npanels;
+    pl.smem = fixed + sizeof(C) * (size_t)pl.panel;
   }
-  if (best < 0) best = 2;
-  pl.in_smem = options[best];
-  pl.smem = bytes(pl.in_smem);
-  pl.ws_stride = (pl.in_smem & kOmSmemD) ? 0 : (pd + 255) & ~size_t(255);
   pl.blocks_per_sm = std::max(1, per_sm(pl.smem));
-  // lanes per segment: about the mean segment length, a power of two <= 32
-  const double mean = (nants + nubls) ? 3.0 * nbls / (nants + nubls) : 1.0;
+  // lanes per segment, a power of two <= 32, from the mean segment length
+  // of a panel: float32 (latency-bound) about its square root; float64
+  // (bound by the FP64 pipe, where each level of the butterfly over the
+  // lanes costs adds) at least OM_GK_D entries a lane
+  const double mean = nseg ? 3.0 * pl.panel / nseg : 1.0;
   int g = 1;
-  while (g < 32 && 2 * g <= mean) g *= 2;
+  if (sizeof(R) == 4)
+    while (g < 32 && 4.0 * g * g <= mean) g *= 2;
+  else
+    while (g < 32 && 2.0 * g * OM_GK_D <= mean) g *= 2;
   pl.group = g;
-  return pl;
+  *out = pl;
+  return HV_OK;
 }
 
 int fail(hv_context* ctx, int code, const char* msg) {
@@ -456,14 +457,8 @@ int fail(hv_context* ctx, int code, const char* msg) {
   return code;
 }
 
-// Incidence lists of the baselines: for antenna a, the baselines with i == a
-// (as is) and j == a (conjugated); for unique baseline k, those with k.
-int build_csr(hv_context* ctx, const uint32_t* ggu, int nbls, int nants, int nubls,
-              std::vector<uint2>& bl, std::vector<int>& off, std::vector<uint32_t>& ent) {
+int check_indices(hv_context* ctx, const uint32_t* ggu, int nbls, int nants, int nubls) {
   char msg[200];
-  bl.resize(nbls);
-  const int nseg = nants + nubls;
-  off.assign(nseg + 1, 0);
   for (int b = 0; b < nbls; ++b) {
     const uint32_t i = ggu[3 * b], j = ggu[3 * b + 1], k = ggu[3 * b + 2];
     if (i >= (uint32_t)nants || j >= (uint32_t)nants || k >= (uint32_t)nubls) {
@@ -471,21 +466,42 @@ int build_csr(hv_context* ctx, const uint32_t* ggu, int nbls, int nants, int nub
                "(%d antennas, %d unique baselines)", b, i, j, k, nants, nubls);
       return fail(ctx, HV_ERR_ARG, msg);
     }
-    bl[b] = make_uint2(i | (j << 16), k);
-    off[i + 1]++;
-    off[j + 1]++;
-    off[nants + k + 1]++;
-  }
-  for (int s = 0; s < nseg; ++s) off[s + 1] += off[s];
-  ent.resize((size_t)off[nseg]);
-  std::vector<int> pos(off.begin(), off.end() - 1);
-  for (int b = 0; b < nbls; ++b) {
-    const uint32_t i = ggu[3 * b], j = ggu[3 * b + 1], k = ggu[3 * b + 2];
-    ent[pos[i]++] = (uint32_t)b;
-    ent[pos[j]++] = (uint32_t)b | 0x80000000u;
-    ent[pos[nants + k]++] = (uint32_t)b;
   }
   return HV_OK;
+}
+
+// Incidence lists of the baselines, one per panel of `panel` baselines: for
+// antenna a, the panel's baselines with i == a (as is) and j == a
+// (conjugated); for unique baseline k, those with k; entries hold the
+// baseline's index within its panel.
+void build_csr(const uint32_t* ggu, int nbls, int nants, int nubls, int panel, int npanels,
+               std::vector<uint2>& bl, std::vector<int>& off, std::vector<uint32_t>& ent) {
+  const int nseg = nants + nubls;
+  bl.resize(nbls);
+  off.assign((size_t)npanels * (nseg + 1), 0);
+  ent.resize((size_t)3 * nbls);
+  size_t base = 0;
+  for (int pn = 0; pn < npanels; ++pn) {
+    const int b0 = pn * panel, b1 = std::min(nbls, b0 + panel);
+    int* o = off.data() + (size_t)pn * (nseg + 1);
+    std::vector<int> cnt(nseg + 1, 0);
+    for (int b = b0; b < b1; ++b) {
+      cnt[ggu[3 * b] + 1]++;
+      cnt[ggu[3 * b + 1] + 1]++;
+      cnt[nants + ggu[3 * b + 2] + 1]++;
+    }
+    o[0] = (int)base;
+    for (int s = 0; s < nseg; ++s) o[s + 1] = o[s] + cnt[s + 1];
+    std::vector<int> pos(o, o + nseg);
+    for (int b = b0; b < b1; ++b) {
+      const uint32_t i = ggu[3 * b], j = ggu[3 * b + 1], k = ggu[3 * b + 2];
+      bl[b] = make_uint2(i | (j << 16), k);
+      ent[pos[i]++] = (uint32_t)(b - b0);
+      ent[pos[j]++] = (uint32_t)(b - b0) | 0x80000000u;
+      ent[pos[nants + k]++] = (uint32_t)(b - b0);
+    }
+    base = (size_t)o[nseg];
+  }
 }
 
 int check_sizes(hv_context* ctx, int precision, int nbls, int nants, int nubls, int ndata,
@@ -506,24 +522,24 @@ int run_typed(hv_context* ctx, const uint32_t* ggu, int nbls, void* d_gains, int
               void* d_ubls, int nubls, const void* d_data, const void* d_wgts, int ndata,
               double conv_crit, int maxiter, int check_every, int check_after, double gain,
               void* d_chisq, uint32_t* d_iters, void* d_conv, cudaStream_t st) {
+  int r = check_indices(ctx, ggu, nbls, nants, nubls);
+  if (r != HV_OK) return r;
+  if (ndata == 0) return HV_OK;
+  Plan pl;
+  if (make_plan<R>(nants, nubls, nbls, &pl) != HV_OK)
+    return fail(ctx, HV_ERR_ARG, "omnical: too many antennas and unique baselines for one CTA");
   std::vector<uint2> bl;
   std::vector<int> off;
   std::vector<uint32_t> ent;
-  int r = build_csr(ctx, ggu, nbls, nants, nubls, bl, off, ent);
-  if (r != HV_OK) return r;
-  if (ndata == 0) return HV_OK;
+  build_csr(ggu, nbls, nants, nubls, pl.panel, pl.npanels, bl, off, ent);
   const int nsm = std::max(1, hv_context_num_sms(ctx));
-  const Plan pl = make_plan<R>(nants, nubls, nbls, 1024);  // 64 registers a thread
-  if (pl.smem > (size_t)kOmSmemLimit && pl.in_smem == 0)
-    return fail(ctx, HV_ERR_ARG, "omnical: too many antennas and unique baselines for one CTA");
   const int grid = std::max(1, std::min(ndata, pl.blocks_per_sm * nsm));
   const size_t n_bl = sizeof(uint2) * bl.size(), n_off = sizeof(int) * off.size(),
                n_ent = sizeof(uint32_t) * ent.size();
   const size_t o_off = (n_bl + 255) & ~size_t(255);
   const size_t o_ent = (o_off + n_off + 255) & ~size_t(255);
   const size_t o_cnt = (o_ent + n_ent + 255) & ~size_t(255);
-  const size_t o_ws = o_cnt + 256;
-  const size_t total = o_ws + pl.ws_stride * (size_t)grid;
+  const size_t total = o_cnt + 256;
   void* buf = nullptr;
   if (cudaMallocAsync(&buf, total, st) != cudaSuccess) {
     cudaGetLastError();
@@ -540,9 +556,8 @@ int run_typed(hv_context* ctx, const uint32_t* ggu, int nbls, void* d_gains, int
   if (r == HV_OK) {
     static bool configured[2] = {false, false};
     if (!configured[sizeof(R) == 8]) {
-      for (const void* k : {reinterpret_cast<const void*>(omnical_kernel<R, 0>),
-                            reinterpret_cast<const void*>(omnical_kernel<R, kOmSmemD>),
-                            reinterpret_cast<const void*>(omnical_kernel<R, kOmSmemD | kOmSmemData>)})
+      for (const void* k : {reinterpret_cast<const void*>(omnical_kernel<R, false>),
+                            reinterpret_cast<const void*>(omnical_kernel<R, true>)})
         if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kOmSmemLimit) !=
             cudaSuccess)
           r = HV_ERR_CUDA;
@@ -556,6 +571,8 @@ int run_typed(hv_context* ctx, const uint32_t* ggu, int nbls, void* d_gains, int
     p.nants = nants;
     p.nubls = nubls;
     p.nbls = nbls;
+    p.panel = pl.panel;
+    p.npanels = pl.npanels;
     p.bl = reinterpret_cast<const uint2*>(b8);
     p.seg_off = reinterpret_cast<const int*>(b8 + o_off);
     p.seg_ent = reinterpret_cast<const uint32_t*>(b8 + o_ent);
@@ -572,15 +589,11 @@ int run_typed(hv_context* ctx, const uint32_t* ggu, int nbls, void* d_gains, int
     p.check_every = check_every;
     p.check_after = check_after;
     p.group = pl.group;
-    p.ws = b8 + o_ws;
-    p.ws_stride = pl.ws_stride;
     p.counter = reinterpret_cast<int*>(b8 + o_cnt);
-    if (pl.in_smem == (kOmSmemD | kOmSmemData))
-      omnical_kernel<R, kOmSmemD | kOmSmemData><<<grid, pl.threads, pl.smem, st>>>(p);
-    else if (pl.in_smem == kOmSmemD)
-      omnical_kernel<R, kOmSmemD><<<grid, pl.threads, pl.smem, st>>>(p);
+    if (pl.data_shared)
+      omnical_kernel<R, true><<<grid, pl.threads, pl.smem, st>>>(p);
     else
-      omnical_kernel<R, 0><<<grid, pl.threads, pl.smem, st>>>(p);
+      omnical_kernel<R, false><<<grid, pl.threads, pl.smem, st>>>(p);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
       hv_context_set_error(ctx, cudaGetErrorString(e));
@@ -634,12 +647,7 @@ int hv_omnical(hv_context* ctx, int precision, const uint32_t* ggu, int nbls, vo
   if (!ctx) return HV_ERR_ARG;
   int r = check_sizes(ctx, precision, nbls, nants, nubls, ndata, maxiter, check_every);
   if (r != HV_OK) return r;
-  if (ndata == 0) {
-    std::vector<uint2> bl;
-    std::vector<int> off;
-    std::vector<uint32_t> ent;
-    return build_csr(ctx, ggu, nbls, nants, nubls, bl, off, ent);
-  }
+  if (ndata == 0) return (nbls > 0 && !ggu) ? HV_ERR_ARG : check_indices(ctx, ggu, nbls, nants, nubls);
   if (!gains || !chisq || !iters || !conv || (nbls > 0 && (!ggu || !data || !wgts)) ||
       (nubls > 0 && !ubls))
     return fail(ctx, HV_ERR_ARG, "omnical: null buffer");
