@@ -573,7 +573,7 @@ def run_median(args, device, steps=5, warmup=3):
 
 
 # the configurations of the reference's own omnical timings
-# (hera_gpu/redcal.py:438-458: 2000 problems, Quadro T2000, the shipped
+# (hera_gpu/redcal.py:431-458: 2000 problems, Quadro T2000, the shipped
 # chunk_size = nthreads // 16): (nants, precision, seconds there)
 OMNICAL_CASES = [(54, 2, 1.5), (126, 2, 5.2), (180, 2, 9.9), (180, 1, 7.3)]
 OMNICAL_NDATA = 2000
@@ -655,7 +655,7 @@ def run_omnical(args, device, steps=3, warmup=3, cpu_sample=8):
                 float((res["iters"][:cpu_sample] == ref["iters"]).mean())
         out.append(case)
     return {"cases": out, "data": "synthetic hex redundant arrays, 1% noise",
-            "reference_published": "hera_gpu/redcal.py:438-458, Quadro T2000, other hardware",
+            "reference_published": "hera_gpu/redcal.py:431-458, Quadro T2000, other hardware",
             "cpu": f"oracle (numpy, 1 process) on {cpu_sample} problems, extrapolated"}
 
 
