@@ -453,9 +453,11 @@ __device__ __forceinline__ void split_pack(const float* v, uint4& hi, uint4& lo)
 // holds the largest |s - s_ref|_1 of the unit (tc_relative_kernel), its sign
 // bit set when all eight sources share a beam pixel (then the four corners
 // are loaded once for the unit).  When
-// that is below dlim = 8 / max_a |U_a|_1 for this slice, the phases are
-// U . s_ref (exact) + U . (s - s_ref), the second term below 8 cycles and so
-// rounded to ~1e-6 cycles in FP32; otherwise every phase is computed exactly.
+// that is below dlim = 32 / max_a |U_a|_1 for this slice, the phases are
+// U . s_ref (exact) + U . (s - s_ref), the second term below 32 cycles and
+// so rounded to a few 1e-6 cycles in FP32 (worst case ~8e-6 cycles, 5e-5
+// rad; the BF16 hi/lo operands carry 16 significant bits, 1.5e-5);
+// otherwise every phase is computed exactly.
 // All lanes read the same records, so the branch does not diverge.  Padding
 // records have zero amplitude.  beam_a: the antenna's column of the
 // transposed beam.
@@ -685,7 +687,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       const Ucoef32* Us = SIM_P(d, U) + (size_t)d.sl * Np;
       const float umax_sl = __ldg(SIM_P(d, umax) + d.sl);
       if (umax_sl >= 4.0e6f && tid == 0) atomicExch(p.err, kErrRange);
-      const float dlim = 8.0f / fmaxf(umax_sl, 1e-30f);
+      const float dlim = 32.0f / fmaxf(umax_sl, 1e-30f);
       const float* beam = SIM_P(d, beamT) + (size_t)d.f * SIM_I(d, PP) * Np;
       // the slots this CTA fills: all of its group's (no clusters) or the
       // ones it owns (cluster mode)
