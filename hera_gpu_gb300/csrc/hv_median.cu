@@ -6,7 +6,8 @@
 // k0 x k1 window (rows x columns; median_filter.py:223-257, FloydWirth_kth on
 // a per-thread copy of the window), one image per stream.
 //
-// Here one launch covers every image of the call.  A block of 8 x 32 output
+// Here one launch covers every image of the call.  3 x 3 windows have their
+// own kernel (median3x3_kernel).  Otherwise a block of 8 x 32 output
 // pixels stages its window tile -- (8 + k0 - 1) x (32 + k1 - 1) values, the
 // zero padding included -- in shared memory as order-preserving 32-bit keys,
 // and each thread finds its pixel's rank-k key with no data-dependent
@@ -116,6 +117,89 @@ median_filter_kernel(const float* __restrict__ in, float* __restrict__ out, int 
   out[(size_t)blockIdx.z * plane + (size_t)r * cols + c] = mf_value(prefix);
 }
 
+// The 3 x 3 window (the reference's default): with each window column
+// sorted into (lo, mid, hi), the median of the nine is
+// med3(max of the three lo, med3 of the three mid, min of the three hi), an
+// exact selection.  A block of 128 x 16 outputs stages its 130 x 18 tile of
+// keys (rows padded to 132 keys, 16-byte aligned); each thread takes 4
+// columns x 2 rows of outputs, so it sorts 6 columns of 4 input rows once
+// (the middle pair shared by both output rows) and reads them with one
+// 128-bit and one 64-bit load per row.
+constexpr int kM3Cols = 128, kM3Rows = 16, kM3Pitch = 132;
+
+__device__ __forceinline__ uint32_t med3u(uint32_t a, uint32_t b, uint32_t c) {
+  return max(min(a, b), min(max(a, b), c));
+}
+
+// vec: rows of the output start 16-byte aligned (cols % 4 == 0 and an
+// aligned base), so whole groups of 4 are stored as one float4.
+__global__ void __launch_bounds__(256) median3x3_kernel(const float* __restrict__ in,
+                                                        float* __restrict__ out, int rows,
+                                                        int cols, bool vec) {
+  __shared__ __align__(16) uint32_t tile[(kM3Rows + 2) * kM3Pitch];
+  const int r0 = (int)blockIdx.y * kM3Rows - 1, c0 = (int)blockIdx.x * kM3Cols - 1;
+  const size_t plane = (size_t)rows * cols;
+  const float* img = in + (size_t)blockIdx.z * plane;
+  const int tid = (int)(threadIdx.y * 32 + threadIdx.x);
+  for (int i = tid; i < (kM3Rows + 2) * (kM3Cols + 2); i += 256) {
+    const int tr = i / (kM3Cols + 2), tc = i - tr * (kM3Cols + 2);
+    const int r = r0 + tr, c = c0 + tc;
+    const float v = (r >= 0 && r < rows && c >= 0 && c < cols) ? img[(size_t)r * cols + c] : 0.f;
+    tile[tr * kM3Pitch + tc] = mf_key(v);
+  }
+  __syncthreads();
+  const int tx = (int)threadIdx.x, ty = (int)threadIdx.y;
+  uint32_t k[4][6];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const uint32_t* row = tile + (2 * ty + i) * kM3Pitch + 4 * tx;
+    const uint4 a = *reinterpret_cast<const uint4*>(row);
+    const uint2 b = *reinterpret_cast<const uint2*>(row + 4);
+    k[i][0] = a.x;
+    k[i][1] = a.y;
+    k[i][2] = a.z;
+    k[i][3] = a.w;
+    k[i][4] = b.x;
+    k[i][5] = b.y;
+  }
+  // sorted columns of input rows 0-2 (output row 0) and 1-3 (output row 1)
+  uint32_t lo[2][6], md[2][6], hi[2][6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const uint32_t p = min(k[1][j], k[2][j]), q = max(k[1][j], k[2][j]);
+#pragma unroll
+    for (int o = 0; o < 2; ++o) {
+      const uint32_t x = k[o ? 3 : 0][j];
+      lo[o][j] = min(p, x);
+      hi[o][j] = max(q, x);
+      md[o][j] = max(p, min(q, x));
+    }
+  }
+  const int c = (int)blockIdx.x * kM3Cols + 4 * tx;
+#pragma unroll
+  for (int o = 0; o < 2; ++o) {
+    const int r = (int)blockIdx.y * kM3Rows + 2 * ty + o;
+    uint32_t v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t mx = max(max(lo[o][q], lo[o][q + 1]), lo[o][q + 2]);
+      const uint32_t mn = min(min(hi[o][q], hi[o][q + 1]), hi[o][q + 2]);
+      v[q] = med3u(mx, med3u(md[o][q], md[o][q + 1], md[o][q + 2]), mn);
+    }
+    if (r < rows) {
+      float* dst = out + (size_t)blockIdx.z * plane + (size_t)r * cols + c;
+      if (vec && c + 3 < cols) {
+        *reinterpret_cast<float4*>(dst) =
+            make_float4(mf_value(v[0]), mf_value(v[1]), mf_value(v[2]), mf_value(v[3]));
+      } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (c + q < cols) dst[q] = mf_value(v[q]);
+      }
+    }
+  }
+}
+
 int check_args(hv_context* ctx, int nimg, int rows, int cols, int k0, int k1, size_t* smem) {
   char msg[256];
   if (nimg < 0 || rows < 0 || cols < 0 || k0 < 1 || k1 < 1 || nimg > 65535 ||
@@ -157,7 +241,12 @@ int launch(hv_context* ctx, const float* d_in, float* d_out, int nimg, int rows,
   const dim3 grid((cols + kMfCols - 1) / kMfCols, (rows + kMfRows - 1) / kMfRows, nimg);
   const dim3 block(kMfCols, kMfRows);
   const int n = k0 * k1;  // the register forms need n / 2 + 1 <= K
-  if (n <= 1) median_filter_kernel<1><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
+  if (k0 == 3 && k1 == 3)
+    median3x3_kernel<<<dim3((cols + kM3Cols - 1) / kM3Cols, (rows + kM3Rows - 1) / kM3Rows, nimg),
+                       dim3(32, 8), 0, st>>>(d_in, d_out, rows, cols,
+                                             (cols & 3) == 0 &&
+                                                 (reinterpret_cast<uintptr_t>(d_out) & 15) == 0);
+  else if (n <= 1) median_filter_kernel<1><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
   else if (n <= 9) median_filter_kernel<5><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
   else if (n <= 25) median_filter_kernel<13><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
   else if (n <= 49) median_filter_kernel<25><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);

@@ -79,3 +79,40 @@ def test_median_filter_even_window_and_bad_window():
                                   median_filter_oracle(img, 4, 2))
     with pytest.raises(_native.HeraVisError):
         MedianFilter(input=img, kernel_size=(301, 301))   # its tile exceeds shared memory
+
+
+@gpu
+@pytest.mark.parametrize("shape", [(16, 128), (17, 129), (31, 130), (33, 131), (2, 4), (300, 517),
+                                   (32, 128), (65, 255)])
+def test_median_3x3_kernel_edges(shape):
+    # the 3 x 3 kernel's block edges (128 x 16 outputs), widths of every
+    # residue mod 4 (float4 stores only when rows are 16-byte aligned),
+    # several images in one launch, ties and negative values
+    from hera_gpu_gb300 import MedianFilter
+    rng = np.random.default_rng(shape[0] * 1000 + shape[1])
+    imgs = np.round(rng.normal(0, 3, (3,) + shape)).astype(np.float32)
+    out = MedianFilter(input=imgs, kernel_size=3)
+    for a, b in zip(imgs, out):
+        np.testing.assert_array_equal(b, median_filter_oracle(a, 3, 3))
+
+
+@gpu
+def test_median_3x3_unaligned_device_output():
+    # hv_median_filter_device into an output that starts 4 bytes past a
+    # 16-byte boundary: the kernel stores element by element
+    import ctypes
+
+    import torch
+    from hera_gpu_gb300 import _native
+    ctx = _native.default_context()
+    img = np.random.default_rng(9).random((40, 64)).astype(np.float32)
+    d_in = torch.from_numpy(img).cuda()
+    d_out = torch.zeros(img.size + 1, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()  # the context's stream does not wait for torch's
+    ctx.check(ctx.lib.hv_median_filter_device(
+        ctx.h, ctypes.c_void_p(d_in.data_ptr()), ctypes.c_void_p(d_out.data_ptr() + 4), 1, 40, 64,
+        3, 3, ctypes.c_void_p(0)))
+    ctx.check(ctx.lib.hv_sync(ctx.h))
+    got = d_out[1:].cpu().numpy().reshape(40, 64)
+    np.testing.assert_array_equal(got, median_filter_oracle(img, 3, 3))
+    assert float(d_out[0]) == 0.0
