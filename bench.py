@@ -194,10 +194,9 @@ def _cpu_worker(args):
     CPU baseline only)."""
     import numpy as np
     from oracle import vis_oracle_partial
-    antpos, freq, eq2top, crd, I, bm = args
+    antpos, freq, eq2top, crd, I, bm, dt = args
     t0 = time.perf_counter()
-    V = vis_oracle_partial(antpos, freq, eq2top, crd, I, bm.astype(np.float64), 0, crd.shape[1],
-                           dtype=np.float64)
+    V = vis_oracle_partial(antpos, freq, eq2top, crd, I, bm.astype(dt), 0, crd.shape[1], dtype=dt)
     return V, time.perf_counter() - t0
 
 
@@ -211,18 +210,20 @@ def cpu_pool():
     return mp.get_context("spawn").Pool(cores), cores
 
 
-def cpu_sample(pool, cores, w, t, f):
+def cpu_sample(pool, cores, w, t, f, dtype="float64"):
     """Oracle on cores x CPU_SAMPLE_SRC sources of slice (t, f), one block of
-    sources per process; returns (V of the sample, seconds, sources).  The
-    seconds are the longest per-process compute time (the parallel span,
-    without the inter-process transfer of inputs)."""
+    sources per process, in float64 (the FP64 oracle) or float32 (the
+    arithmetic of the reference's precision-1 CPU path); returns (V of the
+    sample, seconds, sources).  The seconds are the longest per-process
+    compute time (the parallel span, without the inter-process transfer of
+    inputs)."""
     import numpy as np
     nsamp = min(cores * CPU_SAMPLE_SRC, w["crd_eq"].shape[1])
     bounds = np.linspace(0, nsamp, cores + 1).astype(int)
     a64 = lambda x: np.asarray(x, dtype=np.float64)
     jobs = [(a64(w["antpos"]), float(w["freqs"][f]), a64(w["eq2tops"][t]),
              a64(w["crd_eq"][:, bounds[i]:bounds[i + 1]]), a64(w["I_sky"][bounds[i]:bounds[i + 1]]),
-             np.asarray(w["bm_cubes"][f])) for i in range(cores)]
+             np.asarray(w["bm_cubes"][f]), np.dtype(dtype)) for i in range(cores)]
     parts = pool.map(_cpu_worker, jobs)
     span = max(p[1] for p in parts)
     return sum(p[0] for p in parts), span, nsamp
@@ -423,6 +424,9 @@ def run_ours(args):
                    "method": args.method, "l2": "inputs larger than L2",
                    "parallelism": f"replicas x{world}"},
         "roofline": roof, "clocks": clk, "gpu_launches": launches,
+        # the reference returns the full N x N matrix (the metric above); the
+        # distinct baselines a b >= a of it are N (N + 1) / 2 of those
+        "unique_baselines_per_s": value * (N + 1) / (2.0 * N),
     }
 
     # ---- end to end through the public API, host buffers -----------------
@@ -476,11 +480,14 @@ def run_ours(args):
     # ---- CPU baseline on a bounded sample, and the error of that sample ----
     if rank == 0 and pool is not None:
         V_cpu, wall, nsamp = cpu_sample(pool, cores, w, 0, 0)
+        _, wall32, _ = cpu_sample(pool, cores, w, 0, 0, "float32")
         line["cpu_baseline"] = {
             "value": cpu_rate(wall, nsamp, N, S), "unit": "vis/s", "cores": cores,
             "kind": "port",
+            "value_fp32": cpu_rate(wall32, nsamp, N, S),
             "sample": f"{nsamp} sources of slice (t=0, {w['freqs'][0] / 1e6:.0f} MHz) on {cores} "
-                      f"processes, extrapolated linearly to {S} sources"}
+                      f"processes, extrapolated linearly to {S} sources; value in float64, "
+                      f"value_fp32 in float32"}
         errs = {}
         for method in ("tc", "plain"):
             v = vis_gpu(w["antpos"], float(w["freqs"][0]), w["eq2tops"][:1],
