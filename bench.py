@@ -210,15 +210,15 @@ def cpu_pool():
     return mp.get_context("spawn").Pool(cores), cores
 
 
-def cpu_sample(pool, cores, w, t, f, dtype="float64"):
-    """Oracle on cores x CPU_SAMPLE_SRC sources of slice (t, f), one block of
-    sources per process, in float64 (the FP64 oracle) or float32 (the
+def cpu_sample(pool, cores, w, t, f, dtype="float64", nsamp=None):
+    """Oracle on nsamp (default cores x CPU_SAMPLE_SRC) sources of slice
+    (t, f), one block of sources per process, in float64 (the FP64 oracle) or float32 (the
     arithmetic of the reference's precision-1 CPU path); returns (V of the
     sample, seconds, sources).  The seconds are the longest per-process
     compute time (the parallel span, without the inter-process transfer of
     inputs)."""
     import numpy as np
-    nsamp = min(cores * CPU_SAMPLE_SRC, w["crd_eq"].shape[1])
+    nsamp = min(nsamp or cores * CPU_SAMPLE_SRC, w["crd_eq"].shape[1])
     bounds = np.linspace(0, nsamp, cores + 1).astype(int)
     a64 = lambda x: np.asarray(x, dtype=np.float64)
     jobs = [(a64(w["antpos"]), float(w["freqs"][f]), a64(w["eq2tops"][t]),
@@ -371,6 +371,10 @@ def run_ours(args):
         barrier()
     ms = ev0.elapsed_time(ev1)
     ctx.sync()
+    # one (time, channel) slice of the timed output, for its error against
+    # the FP64 oracle below: channel 0 at the first LST of the last step
+    t_check = times[-1]
+    V_check = {args.method: d_out[0, 0].cpu().numpy()}
     kern_ms, kern_launches = ctx.profile_read()
     ctx.set_profiling(False)
     launches = ctx.launches - l0
@@ -464,10 +468,11 @@ def run_ours(args):
         ctx.profile_read()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        step(1, "plain")
+        t_plain = step(1, "plain")
         e1.record(stream)
         torch.cuda.synchronize(dev)
         pms = e0.elapsed_time(e1)
+        V_check["plain"] = d_out[0, 0].cpu().numpy()
         pk_ms, _ = ctx.profile_read()
         ctx.set_profiling(False)
         pflops = sum(4.0 * N * (N + 1) * sources_up(w, T_PER_STEP + k) * F
@@ -477,24 +482,31 @@ def run_ours(args):
                               "herk_tflops": pflops / (pk_ms / 1e3) / 1e12,
                               "tc_speedup": value / world / (vis_per_step / (pms / 1e3))}
 
-    # ---- CPU baseline on a bounded sample, and the error of that sample ----
+    # ---- CPU baseline: the FP64 oracle of whole slices of the workload,
+    # which also gives the error of the timed output (same inputs, all S
+    # sources, the split-K chunking of the benchmark) ----------------------
     if rank == 0 and pool is not None:
-        V_cpu, wall, nsamp = cpu_sample(pool, cores, w, 0, 0)
-        _, wall32, _ = cpu_sample(pool, cores, w, 0, 0, "float32")
+        V_ref, wall, nsamp = cpu_sample(pool, cores, w, t_check, 0, nsamp=S)
+        _, wall32, nsamp32 = cpu_sample(pool, cores, w, 0, 0, "float32")
         line["cpu_baseline"] = {
             "value": cpu_rate(wall, nsamp, N, S), "unit": "vis/s", "cores": cores,
             "kind": "port",
-            "value_fp32": cpu_rate(wall32, nsamp, N, S),
-            "sample": f"{nsamp} sources of slice (t=0, {w['freqs'][0] / 1e6:.0f} MHz) on {cores} "
-                      f"processes, extrapolated linearly to {S} sources; value in float64, "
-                      f"value_fp32 in float32"}
-        errs = {}
-        for method in ("tc", "plain"):
-            v = vis_gpu(w["antpos"], float(w["freqs"][0]), w["eq2tops"][:1],
-                        w["crd_eq"][:, :nsamp], w["I_sky"][:nsamp], w["bm_cubes"][0],
-                        precision=1, method=method, context=ctx)[0]
-            errs[method] = float(np.linalg.norm(v - V_cpu) / np.linalg.norm(V_cpu))
-        line["rel_err_vs_fp64"] = {**errs, "sample": f"{N} ant x {nsamp} src, one slice"}
+            "value_fp32": cpu_rate(wall32, nsamp32, N, S),
+            "sample": f"value: the float64 oracle of one whole slice (LST {t_check}, "
+                      f"{w['freqs'][0] / 1e6:.0f} MHz, {S} sources) on {cores} processes; "
+                      f"value_fp32: float32 on {nsamp32} sources of a slice, extrapolated "
+                      f"linearly to {S}"}
+        rel = lambda v, r: float(np.linalg.norm(v - r) / np.linalg.norm(r))
+        herm = lambda V: np.triu(V) + np.triu(V, 1).conj().T   # the library's orientation
+        errs = {args.method: rel(V_check[args.method], herm(V_ref))}
+        if "plain" in V_check:
+            V_ref_p = V_ref if t_plain == t_check else \
+                cpu_sample(pool, cores, w, t_plain, 0, nsamp=S)[0]
+            errs["plain"] = rel(V_check["plain"], herm(V_ref_p))
+        line["rel_err_vs_fp64"] = {
+            **errs, "sample": f"one whole slice of the timed output ({N} ant x {S} src, "
+                              f"LST {t_check}, {w['freqs'][0] / 1e6:.0f} MHz) against the FP64 "
+                              f"oracle of the same inputs"}
 
     # ---- batched form: many uneven simulations in one plan ----------------
     if rank == 0 and args.batch_sims > 0:
@@ -799,7 +811,8 @@ def run_serve(args, device, pool):
             ant = full[sel].astype(np.float32).astype(np.float64)
             V = pool.apply(_cpu_worker, ((ant, float(f0), r.eq2tops[0].astype(np.float64),
                                           r.crd_eq.astype(np.float64),
-                                          r.I_sky.astype(np.float64), bm),))[0]
+                                          r.I_sky.astype(np.float64), bm,
+                                          np.dtype(np.float64)),))[0]
             errs.append(float(np.linalg.norm(kept[r.rid] - V) / max(np.linalg.norm(V), 1e-300)))
         out["sample_rel_err_max"] = max(errs)
         out["sample"] = f"{len(errs)} requests, slice (t=0, {sets[0].freqs[0] / 1e6:.0f} MHz)"

@@ -77,6 +77,17 @@ constexpr int TC_GEN_THREADS = TC_GEN_WARPS * 32;
 // their rows, so that 4 (8) stages are generated at once.
 constexpr int TC_TEAM_WARPS = 8;
 constexpr int TC_MAX_STAGES = 8;
+// Stages accumulated in TMEM before the sum is added to the item's split-K
+// partial in global memory (FP32, round to nearest) and the accumulator
+// starts again.  The tensor core's accumulation into TMEM loses a fraction
+// of an ulp of the accumulated value per addition, always toward zero, so
+// its error grows with the number of additions into one value: measured
+// against the FP64 oracle at 350 antennas x 1M sources, the relative error
+// of an autocorrelation summed over 16384 sources is -1e-4, over 1024
+// sources -1.3e-5.  TC_FLUSH_STAGES x TC_KS sources per flush bound it.
+#ifndef TC_FLUSH_STAGES
+#define TC_FLUSH_STAGES 128
+#endif
 constexpr int TC_PRODUCER_WARP = TC_GEN_WARPS;
 constexpr int TC_MMA_WARP = TC_GEN_WARPS + 1;
 constexpr int TC_PUSH_WARP = TC_GEN_WARPS + 2;  // cluster mode: pushes tiles to peer CTAs
@@ -401,6 +412,18 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Adds to global memory without returning the old value (the addition is
+// done at L2, rounded to nearest); one thread's additions and stores to an
+// address take effect in program order.
+__device__ __forceinline__ void red_add(float* p, float v) {
+  asm volatile("red.global.add.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
+}
+__device__ __forceinline__ void red_add4(float4* p, float4 v) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(v.x), "f"(v.y),
+               "f"(v.z), "f"(v.w)
+               : "memory");
+}
+
 __device__ __forceinline__ void sts128(uint32_t addr, uint4 v) {
   asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x), "r"(v.y),
                "r"(v.z), "r"(v.w)
@@ -715,95 +738,119 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       const uint32_t rowoff = (uint32_t)(row >> 3) * 1024u + (uint32_t)r8 * 128u;
       const int wmask = kCluster ? __ldg(&gp->write_mask) : 1;
       bool ok = true;
-      for (int j = 0; j < d.nst && ok && generates; ++j, ++gs) {
-        if ((int)(gs % (uint32_t)nteams) != team) continue;  // another team's stage
-        const int s = (int)(gs % NS);
-        const uint32_t par = (gs / NS) & 1;
-        const int rs = (int)(gs % TC_NREC);
-        if (!wait_warp(rec_full(rs), (gs / TC_NREC) & 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
-        if (!wait_warp<kCluster>(smem_empty(s), par ^ 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
-        const SrcRec32* recs = reinterpret_cast<const SrcRec32*>(rec_smem + (size_t)rs * TC_REC);
-        const uint32_t stage_op = op_base + (uint32_t)s * stage_bytes;
-        auto unit = [&](int i) {
-          const uint32_t tile = stage_op + (uint32_t)u_slot[i] * TC_SLOT + rowoff;
-          uint4 re_h = make_uint4(0, 0, 0, 0), im_h = re_h, re_l = re_h, im_l = re_h;
-          if (u_ok[i]) {
-            float rv[8], iv[8];
-            gen_unit(recs + sg * 8, i == 0 ? uc0 : Us[u_a[i]], beam + u_a[i], Np, dx, dy, dlim,
-                     rv, iv);
-            split_pack(rv, re_h, re_l);
-            split_pack(iv, im_h, im_l);
-          }
-          sts128(tile + ((uint32_t)(sg ^ r8) << 4), re_h);
-          sts128(tile + ((uint32_t)((2 + sg) ^ r8) << 4), im_h);
-          sts128(tile + ((uint32_t)((4 + sg) ^ r8) << 4), re_l);
-          sts128(tile + ((uint32_t)((6 + sg) ^ r8) << 4), im_l);
-        };
-        if (kCluster) {
-          // static unit indices keep the unit tables in registers (a CTA that
-          // generates owns at least one slot)
-          unit(0);
-          if (nfill > 1) unit(1);
-          if (nfill > 2) unit(2);
-        } else {
-#pragma unroll
-          for (int i = 0; i < 3; ++i)
-            if (i < nfill) unit(i);
-        }
-        // operands of this stage written: one arrival per warp (each lane
-        // fences its own writes for the tensor core and the copy engine)
-        fence_async_smem();
-        __syncwarp();
-        if (lane == 0) {
-          mbar_arrive(smem_full(s));
-          if (kCluster) mbar_arrive(gen_done(s));
-          mbar_arrive(rec_empty(rs));  // the records may be reloaded
-        }
-      }
-      if (!ok) break;
-      // ------------------------------------------------------- epilogue --
-      if (!wait_warp(acc_full, ic & 1, abort_flag, p.err, p.wait_ns)) break;
-      tc_fence_after();
-      {
-        // lane quadrant q, 128-column block cb of TMEM: pair cb & 1, plane
-        // cb >> 1 (Re, Im)
-        const int q = warp & 3, cb = warp >> 2;
-        const int pr = cb & 1, plane = cb >> 1;
-        if (pr < g_npairs) {
-          const int I = __ldg(&gp->pI[pr]), J = __ldg(&gp->pJ[pr]);
-          float* out = SIM_P(d, partial) +
-                       (((size_t)d.sl * SIM_I(d, nchunk) + d.k) * 2 + plane) * (size_t)Np * Np;
-          const int a = I * TC_ROWS + q * 32 + lane;
-          if (I <= J) {
-            // partial[b][a] = V[a][b], a contiguous across the warp
-#pragma unroll 1
-            for (int c32 = 0; c32 < 4; ++c32) {
-              float v[32];
-              tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cb * 128 + c32 * 32), v);
-              const int b0 = J * TC_ROWS + c32 * 32;
-#pragma unroll
-              for (int c = 0; c < 32; ++c) out[(size_t)(b0 + c) * Np + a] = v[c];
+      // before reading the accumulator of a flush, generate the first
+      // `ahead` stages of the item's next flush: their operands wait in
+      // shared memory, so the MMAs resume as soon as the accumulator is free.
+      // They reuse buffers that this flush's MMAs release, so they never wait
+      // on the epilogue (ahead <= NS).
+      const int ahead = min(NS, TC_FLUSH_STAGES);
+      int jdone = 0;  // stages of the item generated so far
+      for (int j0 = 0; j0 < d.nst && ok; j0 += TC_FLUSH_STAGES) {
+        const int j1 = min(d.nst, j0 + TC_FLUSH_STAGES);
+        const int jend = min(d.nst, j1 + ahead);
+        for (int j = jdone; j < jend && ok && generates; ++j, ++gs) {
+          if ((int)(gs % (uint32_t)nteams) != team) continue;  // another team's stage
+          const int s = (int)(gs % NS);
+          const uint32_t par = (gs / NS) & 1;
+          const int rs = (int)(gs % TC_NREC);
+          if (!wait_warp(rec_full(rs), (gs / TC_NREC) & 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
+          if (!wait_warp<kCluster>(smem_empty(s), par ^ 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
+          const SrcRec32* recs = reinterpret_cast<const SrcRec32*>(rec_smem + (size_t)rs * TC_REC);
+          const uint32_t stage_op = op_base + (uint32_t)s * stage_bytes;
+          auto unit = [&](int i) {
+            const uint32_t tile = stage_op + (uint32_t)u_slot[i] * TC_SLOT + rowoff;
+            uint4 re_h = make_uint4(0, 0, 0, 0), im_h = re_h, re_l = re_h, im_l = re_h;
+            if (u_ok[i]) {
+              float rv[8], iv[8];
+              gen_unit(recs + sg * 8, i == 0 ? uc0 : Us[u_a[i]], beam + u_a[i], Np, dx, dy, dlim,
+                       rv, iv);
+              split_pack(rv, re_h, re_l);
+              split_pack(iv, im_h, im_l);
             }
+            sts128(tile + ((uint32_t)(sg ^ r8) << 4), re_h);
+            sts128(tile + ((uint32_t)((2 + sg) ^ r8) << 4), im_h);
+            sts128(tile + ((uint32_t)((4 + sg) ^ r8) << 4), re_l);
+            sts128(tile + ((uint32_t)((6 + sg) ^ r8) << 4), im_l);
+          };
+          if (kCluster) {
+            // static unit indices keep the unit tables in registers (a CTA that
+            // generates owns at least one slot)
+            unit(0);
+            if (nfill > 1) unit(1);
+            if (nfill > 2) unit(2);
           } else {
-            // below the diagonal (a > b): partial[a][b] = V[b][a] = conj V[a][b],
-            // 32 consecutive b per lane
-            const float sg = plane ? -1.f : 1.f;
-#pragma unroll 1
-            for (int c32 = 0; c32 < 4; ++c32) {
-              float v[32];
-              tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cb * 128 + c32 * 32), v);
-              float4* o4 = reinterpret_cast<float4*>(out + (size_t)a * Np + J * TC_ROWS + c32 * 32);
 #pragma unroll
-              for (int c = 0; c < 8; ++c)
-                o4[c] = make_float4(sg * v[4 * c], sg * v[4 * c + 1], sg * v[4 * c + 2],
-                                    sg * v[4 * c + 3]);
+            for (int i = 0; i < 3; ++i)
+              if (i < nfill) unit(i);
+          }
+          // operands of this stage written: one arrival per warp (each lane
+          // fences its own writes for the tensor core and the copy engine)
+          fence_async_smem();
+          __syncwarp();
+          if (lane == 0) {
+            mbar_arrive(smem_full(s));
+            if (kCluster) mbar_arrive(gen_done(s));
+            mbar_arrive(rec_empty(rs));  // the records may be reloaded
+          }
+        }
+        if (!ok) break;
+        jdone = jend;
+        // ------------------------------------------------------- epilogue --
+        // the sum of stages [j0, j1): stored into the partial for the first
+        // flush of the item, added to it (at L2, no load) for the later ones
+        const bool first = j0 == 0;
+        if (!wait_warp(acc_full, ic & 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
+        tc_fence_after();
+        {
+          // lane quadrant q, 128-column block cb of TMEM: pair cb & 1, plane
+          // cb >> 1 (Re, Im)
+          const int q = warp & 3, cb = warp >> 2;
+          const int pr = cb & 1, plane = cb >> 1;
+          if (pr < g_npairs) {
+            const int I = __ldg(&gp->pI[pr]), J = __ldg(&gp->pJ[pr]);
+            float* out = SIM_P(d, partial) +
+                         (((size_t)d.sl * SIM_I(d, nchunk) + d.k) * 2 + plane) * (size_t)Np * Np;
+            const int a = I * TC_ROWS + q * 32 + lane;
+            if (I <= J) {
+              // partial[b][a] = V[a][b], a contiguous across the warp
+#pragma unroll 1
+              for (int c32 = 0; c32 < 4; ++c32) {
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cb * 128 + c32 * 32), v);
+                const int b0 = J * TC_ROWS + c32 * 32;
+                if (first) {
+#pragma unroll
+                  for (int c = 0; c < 32; ++c) out[(size_t)(b0 + c) * Np + a] = v[c];
+                } else {
+#pragma unroll
+                  for (int c = 0; c < 32; ++c) red_add(out + (size_t)(b0 + c) * Np + a, v[c]);
+                }
+              }
+            } else {
+              // below the diagonal (a > b): partial[a][b] = V[b][a] = conj V[a][b],
+              // 32 consecutive b per lane
+              const float sg = plane ? -1.f : 1.f;
+#pragma unroll 1
+              for (int c32 = 0; c32 < 4; ++c32) {
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cb * 128 + c32 * 32), v);
+                float4* o4 = reinterpret_cast<float4*>(out + (size_t)a * Np + J * TC_ROWS + c32 * 32);
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                  const float4 x = make_float4(sg * v[4 * c], sg * v[4 * c + 1],
+                                               sg * v[4 * c + 2], sg * v[4 * c + 3]);
+                  if (first) o4[c] = x;
+                  else red_add4(o4 + c, x);
+                }
+              }
             }
           }
         }
-      }
-      tc_fence_before();
-      mbar_arrive(acc_empty);
-      ++ic;
+        tc_fence_before();
+        mbar_arrive(acc_empty);
+        ++ic;
+      }  // flushes of the item
+      if (!ok) break;
     }
   } else if (warp == TC_PRODUCER_WARP) {
     // ----------------------------------------------------- TMA producer --
@@ -845,26 +892,30 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
         const uint32_t idp = idesc_bf16(nm, false), idn = idesc_bf16(nm, true);
         const uint32_t a0 = desc_lo(op_base + (uint32_t)__ldg(&gp->sa) * TC_SLOT);
         const uint32_t b0 = desc_lo(op_base);
-        if (!wait1(acc_empty, (ic & 1) ^ 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
-        tc_fence_after();
-        for (int j = 0; j < d.nst; ++j, ++gs) {
-          const int s = (int)(gs % NS);
-          const uint32_t par = (gs / NS) & 1;
-          if (!wait1(smem_full(s), par, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
-          // arm the next round of this stage for the peers' pushes (they can
-          // only come after this round's MMAs release the slot)
-          if (recv_bytes) mbar_expect_tx(smem_full(s), recv_bytes);
+        for (int j0 = 0; j0 < d.nst && ok; j0 += TC_FLUSH_STAGES) {
+          const int j1 = min(d.nst, j0 + TC_FLUSH_STAGES);
+          // the generators have read the accumulator of the last flush
+          if (!wait1(acc_empty, (ic & 1) ^ 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
           tc_fence_after();
-          const uint32_t so = ((uint32_t)s * stage_bytes) >> 4;
-          issue_group(tmem, a0 + so, b0 + so, idp, idn, j == 0);
-          // the stage's slots may be refilled -- here and, in cluster mode,
-          // by the CTAs that wrote them -- once these MMAs have read them
-          if (kCluster && cmask != (uint16_t)(1u << rank)) mma_commit_multicast(smem_empty(s), cmask);
-          else mma_commit(smem_empty(s));
-        }
-        if (!ok) break;
-        mma_commit(acc_full);
-        ++ic;
+          for (int j = j0; j < j1; ++j, ++gs) {
+            const int s = (int)(gs % NS);
+            const uint32_t par = (gs / NS) & 1;
+            if (!wait1(smem_full(s), par, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
+            // arm the next round of this stage for the peers' pushes (they can
+            // only come after this round's MMAs release the slot)
+            if (recv_bytes) mbar_expect_tx(smem_full(s), recv_bytes);
+            tc_fence_after();
+            const uint32_t so = ((uint32_t)s * stage_bytes) >> 4;
+            issue_group(tmem, a0 + so, b0 + so, idp, idn, j == j0);
+            // the stage's slots may be refilled -- here and, in cluster mode,
+            // by the CTAs that wrote them -- once these MMAs have read them
+            if (kCluster && cmask != (uint16_t)(1u << rank)) mma_commit_multicast(smem_empty(s), cmask);
+            else mma_commit(smem_empty(s));
+          }
+          if (!ok) break;
+          mma_commit(acc_full);
+          ++ic;
+        }  // flushes of the item
       }
       // every MMA issued by this thread completes before TMEM is released
       mma_commit(drain);
