@@ -44,10 +44,49 @@ __device__ __forceinline__ float mf_value(uint32_t k) {
   return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
 }
 
+__device__ __forceinline__ uint32_t med3u(uint32_t a, uint32_t b, uint32_t c) {
+  return max(min(a, b), min(max(a, b), c));
+}
+
+// Median of a W x W window (W odd) by forgetful selection: the first
+// W^2 / 2 + 2 keys are held in registers; for each further key the buffer's
+// maximum is bubbled to its top and its minimum to its bottom, both are
+// dropped (neither can be the median: each has more than W^2 / 2 keys on
+// its other side, counting the keys dropped before) and the new key takes
+// the maximum's place.  The median of the three keys left is the window's.
+// About 2 W^4 / 4 min/max operations, against 2 (W^2 / 2 + 1) W^2 for the
+// register insertion below.
+template <int W>
+__device__ __forceinline__ uint32_t forgetful_median(const uint32_t* win, int tw) {
+  constexpr int N = W * W, R0 = N / 2 + 2;
+  uint32_t a[R0];
+#pragma unroll
+  for (int e = 0; e < R0; ++e) a[e] = win[(e / W) * tw + e % W];
+#pragma unroll
+  for (int e = R0; e < N; ++e) {
+    const int lo = e - R0;  // the buffer is a[lo .. R0 - 1]
+#pragma unroll
+    for (int i = lo; i < R0 - 1; ++i) {
+      const uint32_t x = min(a[i], a[i + 1]);
+      a[i + 1] = max(a[i], a[i + 1]);
+      a[i] = x;
+    }
+#pragma unroll
+    for (int i = R0 - 2; i > lo; --i) {
+      const uint32_t x = min(a[i - 1], a[i]);
+      a[i] = max(a[i - 1], a[i]);
+      a[i - 1] = x;
+    }
+    a[R0 - 1] = win[(e / W) * tw + e % W];
+  }
+  return med3u(a[R0 - 3], a[R0 - 2], a[R0 - 1]);
+}
+
 // grid (ceil(cols / 32), ceil(rows / 8), nimg), block (32, 8); dynamic shared
-// memory (8 + k0 - 1) * (32 + k1 - 1) keys.  K > 0: windows of at most
-// 2 K - 1 elements select with K registers; K == 0: radix select.
-template <int K>
+// memory (8 + k0 - 1) * (32 + k1 - 1) keys.  W > 0: a W x W window by
+// forgetful selection; else K > 0: windows of at most 2 K - 1 elements
+// select with K registers; K == 0: radix select.
+template <int K, int W = 0>
 __global__ void __launch_bounds__(kMfCols * kMfRows)
 median_filter_kernel(const float* __restrict__ in, float* __restrict__ out, int rows, int cols,
                      int k0, int k1) {
@@ -69,6 +108,10 @@ median_filter_kernel(const float* __restrict__ in, float* __restrict__ out, int 
   if (r >= rows || c >= cols) return;
   const uint32_t* win = tile + threadIdx.y * tw + threadIdx.x;
   const int rank = (k0 * k1) / 2;
+  if (W > 0) {
+    out[(size_t)blockIdx.z * plane + (size_t)r * cols + c] = mf_value(forgetful_median<W>(win, tw));
+    return;
+  }
   if (K > 0) {
     // s[0..K) holds the smallest keys seen so far, ascending; a new key
     // sinks to its place and the largest falls out
@@ -126,10 +169,6 @@ median_filter_kernel(const float* __restrict__ in, float* __restrict__ out, int 
 // (the middle pair shared by both output rows) and reads them with one
 // 128-bit and one 64-bit load per row.
 constexpr int kM3Cols = 128, kM3Rows = 16, kM3Pitch = 132;
-
-__device__ __forceinline__ uint32_t med3u(uint32_t a, uint32_t b, uint32_t c) {
-  return max(min(a, b), min(max(a, b), c));
-}
 
 // vec: rows of the output start 16-byte aligned (cols % 4 == 0 and an
 // aligned base), so whole groups of 4 are stored as one float4.
@@ -232,7 +271,10 @@ int launch(hv_context* ctx, const float* d_in, float* d_out, int nimg, int rows,
                           reinterpret_cast<const void*>(median_filter_kernel<5>),
                           reinterpret_cast<const void*>(median_filter_kernel<13>),
                           reinterpret_cast<const void*>(median_filter_kernel<25>),
-                          reinterpret_cast<const void*>(median_filter_kernel<41>)})
+                          reinterpret_cast<const void*>(median_filter_kernel<41>),
+                          reinterpret_cast<const void*>(median_filter_kernel<0, 5>),
+                          reinterpret_cast<const void*>(median_filter_kernel<0, 7>),
+                          reinterpret_cast<const void*>(median_filter_kernel<0, 9>)})
       if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kMfSmemLimit) !=
           cudaSuccess)
         return HV_ERR_CUDA;
@@ -246,6 +288,12 @@ int launch(hv_context* ctx, const float* d_in, float* d_out, int nimg, int rows,
                        dim3(32, 8), 0, st>>>(d_in, d_out, rows, cols,
                                              (cols & 3) == 0 &&
                                                  (reinterpret_cast<uintptr_t>(d_out) & 15) == 0);
+  else if (k0 == 5 && k1 == 5)
+    median_filter_kernel<0, 5><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
+  else if (k0 == 7 && k1 == 7)
+    median_filter_kernel<0, 7><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
+  else if (k0 == 9 && k1 == 9)
+    median_filter_kernel<0, 9><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
   else if (n <= 1) median_filter_kernel<1><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
   else if (n <= 9) median_filter_kernel<5><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
   else if (n <= 25) median_filter_kernel<13><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
