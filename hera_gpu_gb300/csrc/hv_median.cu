@@ -48,17 +48,18 @@ __device__ __forceinline__ uint32_t med3u(uint32_t a, uint32_t b, uint32_t c) {
   return max(min(a, b), min(max(a, b), c));
 }
 
-// Median of a W x W window (W odd) by forgetful selection: the first
-// W^2 / 2 + 2 keys are held in registers; for each further key the buffer's
-// maximum is bubbled to its top and its minimum to its bottom, both are
-// dropped (neither can be the median: each has more than W^2 / 2 keys on
+// Median of an H x W window (H W odd) by forgetful selection: the first
+// n / 2 + 2 keys (n = H W) are held in registers; for each further key the
+// buffer's maximum is bubbled to its top and its minimum to its bottom, both
+// are dropped (neither can be the median: each has more than n / 2 keys on
 // its other side, counting the keys dropped before) and the new key takes
 // the maximum's place.  The median of the three keys left is the window's.
-// About 2 W^4 / 4 min/max operations, against 2 (W^2 / 2 + 1) W^2 for the
+// About n^2 / 2 min/max operations, against 2 (n / 2 + 1) n for the
 // register insertion below.
-template <int W>
+template <int H, int W>
 __device__ __forceinline__ uint32_t forgetful_median(const uint32_t* win, int tw) {
-  constexpr int N = W * W, R0 = N / 2 + 2;
+  constexpr int N = H * W, R0 = N / 2 + 2;
+  static_assert(N % 2 == 1 && N >= 3, "odd windows of at least 3 keys");
   uint32_t a[R0];
 #pragma unroll
   for (int e = 0; e < R0; ++e) a[e] = win[(e / W) * tw + e % W];
@@ -83,10 +84,10 @@ __device__ __forceinline__ uint32_t forgetful_median(const uint32_t* win, int tw
 }
 
 // grid (ceil(cols / 32), ceil(rows / 8), nimg), block (32, 8); dynamic shared
-// memory (8 + k0 - 1) * (32 + k1 - 1) keys.  W > 0: a W x W window by
-// forgetful selection; else K > 0: windows of at most 2 K - 1 elements
-// select with K registers; K == 0: radix select.
-template <int K, int W = 0>
+// memory (8 + k0 - 1) * (32 + k1 - 1) keys.  H > 0: an H x W window (k0 = H,
+// k1 = W) by forgetful selection; else K > 0: windows of at most 2 K - 1
+// elements select with K registers; K == 0: radix select.
+template <int K, int H = 0, int W = 0>
 __global__ void __launch_bounds__(kMfCols * kMfRows)
 median_filter_kernel(const float* __restrict__ in, float* __restrict__ out, int rows, int cols,
                      int k0, int k1) {
@@ -108,8 +109,8 @@ median_filter_kernel(const float* __restrict__ in, float* __restrict__ out, int 
   if (r >= rows || c >= cols) return;
   const uint32_t* win = tile + threadIdx.y * tw + threadIdx.x;
   const int rank = (k0 * k1) / 2;
-  if (W > 0) {
-    out[(size_t)blockIdx.z * plane + (size_t)r * cols + c] = mf_value(forgetful_median<W>(win, tw));
+  if constexpr (H > 0) {
+    out[(size_t)blockIdx.z * plane + (size_t)r * cols + c] = mf_value(forgetful_median<H, W>(win, tw));
     return;
   }
   if (K > 0) {
@@ -272,9 +273,11 @@ int launch(hv_context* ctx, const float* d_in, float* d_out, int nimg, int rows,
                           reinterpret_cast<const void*>(median_filter_kernel<13>),
                           reinterpret_cast<const void*>(median_filter_kernel<25>),
                           reinterpret_cast<const void*>(median_filter_kernel<41>),
-                          reinterpret_cast<const void*>(median_filter_kernel<0, 5>),
-                          reinterpret_cast<const void*>(median_filter_kernel<0, 7>),
-                          reinterpret_cast<const void*>(median_filter_kernel<0, 9>)})
+                          reinterpret_cast<const void*>(median_filter_kernel<0, 5, 5>),
+                          reinterpret_cast<const void*>(median_filter_kernel<0, 7, 7>),
+                          reinterpret_cast<const void*>(median_filter_kernel<0, 9, 9>),
+                          reinterpret_cast<const void*>(median_filter_kernel<0, 9, 5>),
+                          reinterpret_cast<const void*>(median_filter_kernel<0, 5, 9>)})
       if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kMfSmemLimit) !=
           cudaSuccess)
         return HV_ERR_CUDA;
@@ -289,11 +292,15 @@ int launch(hv_context* ctx, const float* d_in, float* d_out, int nimg, int rows,
                                              (cols & 3) == 0 &&
                                                  (reinterpret_cast<uintptr_t>(d_out) & 15) == 0);
   else if (k0 == 5 && k1 == 5)
-    median_filter_kernel<0, 5><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
+    median_filter_kernel<0, 5, 5><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
   else if (k0 == 7 && k1 == 7)
-    median_filter_kernel<0, 7><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
+    median_filter_kernel<0, 7, 7><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
   else if (k0 == 9 && k1 == 9)
-    median_filter_kernel<0, 9><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
+    median_filter_kernel<0, 9, 9><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
+  else if (k0 == 9 && k1 == 5)
+    median_filter_kernel<0, 9, 5><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
+  else if (k0 == 5 && k1 == 9)
+    median_filter_kernel<0, 5, 9><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
   else if (n <= 1) median_filter_kernel<1><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
   else if (n <= 9) median_filter_kernel<5><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);
   else if (n <= 25) median_filter_kernel<13><<<grid, block, smem, st>>>(d_in, d_out, rows, cols, k0, k1);

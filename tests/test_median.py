@@ -119,14 +119,14 @@ def test_median_3x3_unaligned_device_output():
 
 
 @gpu
-@pytest.mark.parametrize("w", [5, 7, 9])
+@pytest.mark.parametrize("ks", [(5, 5), (7, 7), (9, 9), (9, 5), (5, 9)])
 @pytest.mark.parametrize("shape", [(1, 1), (13, 11), (61, 47), (300, 129)])
-def test_median_square_windows_forgetful(w, shape):
-    # the 5 x 5, 7 x 7 and 9 x 9 windows (forgetful selection): ties,
-    # negative values, zero padding at every edge, several images a launch
+def test_median_windows_forgetful(ks, shape):
+    # the windows taken by forgetful selection: ties, negative values, zero
+    # padding at every edge, several images a launch
     from hera_gpu_gb300 import MedianFilter
-    rng = np.random.default_rng(w * 100 + shape[0])
+    rng = np.random.default_rng(ks[0] * 1000 + ks[1] * 100 + shape[0])
     imgs = np.round(rng.normal(0, 2, (2,) + shape)).astype(np.float32)
-    out = MedianFilter(input=imgs, kernel_size=w)
+    out = MedianFilter(input=imgs, kernel_size=ks)
     for a, b in zip(imgs, out):
-        np.testing.assert_array_equal(b, median_filter_oracle(a, w, w))
+        np.testing.assert_array_equal(b, median_filter_oracle(a, *ks))
