@@ -22,10 +22,10 @@
 // a counter), every iteration inside the kernel, the solution and the
 // per-baseline values in shared memory (a panel of baselines at a time when
 // they do not all fit), the model recomputed from the solution where it is
-// needed.  The sums over each antenna's and each unique
-// baseline's baselines are gathers over a fixed incidence list (CSR), each
-// segment summed by a fixed group of lanes in a fixed order, so the result
-// does not depend on scheduling and repeats bit for bit.
+// needed.  The sums over each antenna's and each unique baseline's
+// baselines are gathers over a fixed incidence list (CSR), each segment
+// summed by a fixed group of lanes in a fixed order, so the result does not
+// depend on scheduling and repeats bit for bit.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -42,7 +42,12 @@ template <typename R> struct Cx;
 template <> struct Cx<float> { using T = float2; };
 template <> struct Cx<double> { using T = double2; };
 
-constexpr int kOmMaxThreads = 512;
+// Launch and loop shape, as measured best on GB300 (float32 / float64):
+//   OM_UNROLL_*  baselines a thread takes per pass of the per-baseline loops
+//   OM_GATHER_*  incidence entries a lane loads ahead in the segment gathers
+//   OM_MINB      CTAs of 512 threads an SM (2: 64 registers a thread)
+//   OM_GK_D      float64 gathers: at least this many entries a lane
+//   OM_WANT_*    CTAs of 512 threads an SM the panels of baselines are sized for
 #ifndef OM_UNROLL_F
 #define OM_UNROLL_F 1
 #define OM_UNROLL_D 1
@@ -50,17 +55,18 @@ constexpr int kOmMaxThreads = 512;
 #define OM_GATHER_D 2
 #endif
 #ifndef OM_MINB
-#define OM_MINB 2  // CTAs of 512 threads an SM: 64 registers a thread
+#define OM_MINB 2
 #endif
-constexpr int kOmSmemLimit = 226 * 1024;  // dynamic shared memory, below the 227 KB per CTA
-constexpr int kOmThreadsPerSm = 1024 * (OM_MINB > 2 ? 2 : OM_MINB) / 2;  // register limit
 #ifndef OM_GK_D
-#define OM_GK_D 16  // float64 gathers: entries a lane at least
+#define OM_GK_D 16
 #endif
 #ifndef OM_WANT_F
-#define OM_WANT_F 2  // CTAs of 512 threads an SM the panels are sized for
+#define OM_WANT_F 2
 #define OM_WANT_D 2
 #endif
+constexpr int kOmMaxThreads = 512;
+constexpr int kOmSmemLimit = 226 * 1024;  // dynamic shared memory, below the 227 KB per CTA
+constexpr int kOmThreadsPerSm = 1024 * (OM_MINB > 2 ? 2 : OM_MINB) / 2;  // register limit
 
 template <typename R>
 struct OmParams {
