@@ -77,3 +77,35 @@ def test_precision_must_be_1_or_2():
     with pytest.raises(AssertionError):
         vis_gpu(np.zeros((2, 3)), 0.15, np.zeros((1, 3, 3)), np.zeros((3, 4)), np.zeros(4),
                 np.zeros((2, 3, 3)), precision=3)
+
+
+def test_omnical_asserts_before_any_device_work():
+    # redcal.py:392-402 of the reference
+    from hera_gpu_gb300 import omnical
+    ggu = np.array([(1, 0, 0)], dtype=np.uint32)
+    g, u, d, w = np.ones((2, 2)), np.ones((2, 1)), np.ones((2, 1)), np.ones((2, 1))
+    for kw in (dict(ggu_indices=ggu.T), dict(check_every=1), dict(precision=3),
+               dict(data=np.ones((2, 2))), dict(wgts=np.ones((3, 1))), dict(ubls=np.ones(2))):
+        args = dict(ggu_indices=ggu, gains=g, ubls=u, data=d, wgts=w)
+        extra = {k: v for k, v in kw.items() if k not in args}
+        args.update({k: v for k, v in kw.items() if k in args})
+        with pytest.raises((AssertionError, IndexError)):
+            omnical(**args, **extra)
+
+
+def test_median_filter_asserts_before_any_device_work():
+    from hera_gpu_gb300 import MedianFilter
+    with pytest.raises(AssertionError):
+        MedianFilter(input=np.zeros((4, 4)), kernel_size=0)
+    with pytest.raises(AssertionError):
+        MedianFilter(input=np.zeros(4), kernel_size=3)
+
+
+def test_entry_points_reject_a_null_context(lib):
+    # HV_ERR_ARG (1), without touching CUDA
+    assert lib.hv_omnical(None, 1, None, 0, None, 0, None, 0, None, None, 0, 1e-10, 50, 4, 1,
+                          0.3, None, None, None) == 1
+    assert lib.hv_omnical_device(None, 1, None, 0, None, 0, None, 0, None, None, 0, 1e-10, 50,
+                                 4, 1, 0.3, None, None, None, None) == 1
+    assert lib.hv_median_filter(None, None, None, 0, 0, 0, 3, 3) == 1
+    assert lib.hv_median_filter_device(None, None, None, 0, 0, 0, 3, 3, None) == 1
