@@ -12,8 +12,10 @@ window's element of rank floor(k0 * k1 / 2) in ascending order
 
 Pinned by the reference's own test oracle (hera_gpu/tests/test_median_filter.py
 compares with scipy.signal.medfilt2d), which agrees with this restatement for
-odd windows; tests/test_median.py checks that.  Only tests/ and bench.py's CPU
-baseline use this module.
+odd windows, and by the reference's own MedianFilter run on the CPU
+(oracle/median_ref.py; tests/golden/median_reference.npz), bit for bit for
+odd, even and one-dimensional windows; tests/test_median.py checks both.
+Only tests/ and bench.py's CPU baseline use this module.
 """
 import numpy as np
 

@@ -8,14 +8,12 @@ GPU, to produce reference outputs for tests/golden/ (make_omnical_golden.py):
   (zero-filled, where pycuda's gpuarray.empty leaves memory as it finds it),
   events are no-ops, the two cuBLAS copies are memory copies, and the
   hera_cal / linsolve names its wrapper classes use are placeholders;
-* ``SourceModule`` formats nothing itself: it takes the kernel source exactly
-  as the reference formats it, adds a prelude that defines the CUDA
-  built-ins for the host (blockIdx / threadIdx as globals, atomicAdd as a
-  plain addition, __syncthreads as nothing), compiles it with g++ into
-  oracle/_ref/, and runs a launch as a loop over every thread -- blocks
-  y-major, then threads y-major, so that in update_active (redcal.py:314-354)
-  the thread with td == 0 of a pixel runs before the others that read the
-  flag it writes, as the kernel's barrier orders them.
+* ``SourceModule`` is oracle/cuda_emu.py: the kernel source exactly as the
+  reference formats it, compiled with g++ for the host, a launch run as a
+  loop over every thread -- blocks y-major, then threads y-major, so that in
+  update_active (redcal.py:314-354) the thread with td == 0 of a pixel runs
+  before the others that read the flag it writes, as the kernel's barrier
+  orders them.
 
 The atomic sums are thus taken in thread order, which the GPU does not fix;
 their rounding differs from any one GPU run at the last bits.  Needs the
@@ -25,36 +23,17 @@ from __future__ import annotations
 
 import contextlib
 import ctypes
-import hashlib
 import importlib.util
 import os
-import re
-import subprocess
 import sys
 import types
 
 import numpy as np
 
-HERE = os.path.dirname(os.path.abspath(__file__))
-OUT = os.path.join(HERE, "_ref")
-CUDA_INCLUDE = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+from . import cuda_emu
 
-PRELUDE = r"""
-#define __CUDA_ARCH__ 800  /* skips the template's atomicAdd(double) shim */
-#include <cmath>
-#include <cstdio>
-#include <cuComplex.h>
-#undef __global__
-#define __global__ static
-typedef unsigned int uint;
-struct EmuDim3 { unsigned x, y, z; };
-static EmuDim3 blockIdx, threadIdx, blockDim, gridDim;
-#define __syncthreads()
-static inline float atomicAdd(float* a, float v) { float o = *a; *a = o + v; return o; }
-static inline double atomicAdd(double* a, double v) { double o = *a; *a = o + v; return o; }
-"""
-
-_SCALAR = {"uint": ctypes.c_uint, "float": ctypes.c_float, "double": ctypes.c_double}
+# the template's atomicAdd(double) shim is for devices before sm_60
+_DEFINES = "#define __CUDA_ARCH__ 800\n"
 
 
 class _GPUArray:
@@ -83,74 +62,8 @@ class _Event:
         return 0.0
 
 
-def _parse_kernels(code):
-    """[(name, [(scalar type or None for a pointer, declared type, name)])] of
-    every kernel of the formatted template."""
-    out = []
-    for name, params in re.findall(r"__global__\s+void\s+(\w+)\s*\(([^)]*)\)", code, re.S):
-        ps = []
-        for p in params.split(","):
-            p = " ".join(p.split())
-            pname = re.findall(r"(\w+)\s*$", p)[0]
-            ptype = p[: -len(pname)].strip()
-            ps.append((None if "*" in ptype else ptype, ptype, pname))
-        out.append((name, ps))
-    return out
-
-
-class _Kernel:
-    def __init__(self, fn, params):
-        self.fn, self.params = fn, params
-        fn.restype = None
-        fn.argtypes = [ctypes.c_uint] * 5 + [ctypes.c_void_p if s is None else _SCALAR[s]
-                                             for s, _, _ in params]
-
-    def __call__(self, *args, block, grid):
-        conv = []
-        for (s, _, _), a in zip(self.params, args):
-            if s is None:
-                conv.append(ctypes.c_void_p(a.arr.ctypes.data))
-            else:
-                conv.append(_SCALAR[s](a.item() if hasattr(a, "item") else a))
-        gx, gy = (tuple(grid) + (1, 1))[:2]
-        bx, by, bz = (tuple(block) + (1, 1, 1))[:3]
-        self.fn(gx, gy, bx, by, bz, *conv)
-
-
-class _SourceModule:
-    def __init__(self, code):
-        kernels = _parse_kernels(code)
-        wrappers = []
-        for name, ps in kernels:
-            decl = ", ".join(f"{t} {n}" for _, t, n in ps)
-            call = ", ".join(n for _, _, n in ps)
-            wrappers.append(
-                f'extern "C" void emu_{name}(unsigned gx, unsigned gy, unsigned tbx, unsigned tby, '
-                f"unsigned tbz{', ' if decl else ''}{decl}) {{\n"
-                "  gridDim = {gx, gy, 1u}; blockDim = {tbx, tby, tbz};\n"
-                "  for (unsigned y = 0; y < gy; ++y) for (unsigned x = 0; x < gx; ++x) {\n"
-                "    blockIdx = {x, y, 0u};\n"
-                "    for (unsigned tz = 0; tz < tbz; ++tz) for (unsigned ty = 0; ty < tby; ++ty)\n"
-                "      for (unsigned tx = 0; tx < tbx; ++tx) {\n"
-                f"        threadIdx = {{tx, ty, tz}}; {name}({call});\n"
-                "      }\n  }\n}\n")
-        src = PRELUDE + code + "\n" + "".join(wrappers)
-        key = hashlib.sha256(src.encode()).hexdigest()[:16]
-        os.makedirs(OUT, exist_ok=True)
-        inc = os.path.join(OUT, "include")
-        os.makedirs(inc, exist_ok=True)
-        open(os.path.join(inc, "pycuda-helpers.hpp"), "w").close()
-        so = os.path.join(OUT, f"redcal_kernels_{key}.so")
-        if not os.path.exists(so):
-            cpp = so[:-3] + ".cpp"
-            open(cpp, "w").write(src)
-            subprocess.run(["g++", "-O2", "-shared", "-fPIC", "-w", "-I", CUDA_INCLUDE, "-I", inc,
-                            cpp, "-o", so], check=True)
-        lib = ctypes.CDLL(so)
-        self.kernels = {name: _Kernel(getattr(lib, f"emu_{name}"), ps) for name, ps in kernels}
-
-    def get_function(self, name):
-        return self.kernels[name]
+def _source_module(code):
+    return cuda_emu.Module(code, includes="#include <cuComplex.h>", defines=_DEFINES)
 
 
 def _copy(itemsize):
@@ -169,7 +82,7 @@ def _stubs():
         m = types.ModuleType("pycuda." + sub)
         setattr(pycuda, sub, m)
         mods["pycuda." + sub] = m
-    mods["pycuda.compiler"].SourceModule = _SourceModule
+    mods["pycuda.compiler"].SourceModule = _source_module
     mods["pycuda.gpuarray"].empty = lambda shape, dtype: _GPUArray(shape, dtype)
     mods["pycuda.driver"].Event = _Event
     skcuda = types.ModuleType("skcuda")

@@ -2,10 +2,13 @@
 
 CPU: the oracle restatement against scipy.signal.medfilt2d, the reference's
 own test oracle (hera_gpu/tests/test_median_filter.py), including 1x1
-images and windows larger than the image.  GPU: the library's kernel against
+images and windows larger than the image, and against the reference's own
+MedianFilter run on the CPU (tests/golden/median_reference.npz, made by
+make_median_golden.py), which also covers even windows.  GPU: the library's kernel against
 the oracle, bit for bit (a median is a selection, no arithmetic), on the
 reference's test shapes and windows, through the drop-in MedianFilter.
 """
+import os
 import zlib
 
 import numpy as np
@@ -13,6 +16,19 @@ import pytest
 import scipy.signal as sps
 
 from oracle import median_filter_oracle
+
+GOLDEN = np.load(os.path.join(os.path.dirname(__file__), "golden", "median_reference.npz"))
+REF_CASES = sorted(int(k[3:]) for k in GOLDEN.files if k.startswith("in_"))
+
+
+@pytest.mark.parametrize("n", REF_CASES)
+def test_oracle_matches_the_reference_median_filter(n):
+    # the reference's own MedianFilter (its mf kernel, run on the CPU) on odd,
+    # even and one-dimensional windows: equal bit for bit
+    k0, k1 = (int(x) for x in GOLDEN[f"window_{n}"])
+    for img, ref in zip(GOLDEN[f"in_{n}"], GOLDEN[f"out_{n}"]):
+        np.testing.assert_array_equal(median_filter_oracle(img, k0, k1), ref)
+
 
 ODD_CASES = [((1, 1), 1), ((29, 29), 1), ((29, 29), 3), ((93, 93), 3), ((1, 1), 3),
              ((1, 1), 9), ((40, 37), 5), ((1, 73), (1, 11)), ((5, 3), (11, 1)),
@@ -58,6 +74,18 @@ def test_median_filter_matches_oracle(shape, ks):
         median_filter_oracle(img, k0, k1)
     np.testing.assert_array_equal(out[0], ref)
     assert np.allclose(sps.medfilt2d(img, (k0, k1)), out)   # the reference's own check
+
+
+@gpu
+@pytest.mark.parametrize("n", REF_CASES)
+def test_median_filter_matches_the_reference(n):
+    # the library against the reference's own MedianFilter, bit for bit
+    from hera_gpu_gb300 import MedianFilter
+    k0, k1 = (int(x) for x in GOLDEN[f"window_{n}"])
+    imgs = GOLDEN[f"in_{n}"]
+    out = MedianFilter(input=imgs, kernel_size=(k0, k1))
+    for got, ref in zip(out, GOLDEN[f"out_{n}"]):
+        np.testing.assert_array_equal(got, ref)
 
 
 @gpu
