@@ -321,7 +321,7 @@ def run_ours(args):
     if rank == 0 and not args.no_cpu:
         pool, cores = cpu_pool()      # spawned before the first CUDA call
     import torch
-    from hera_gpu_gb300 import _native, vis_gpu, vis_gpu_multifreq
+    from hera_gpu_gb300 import _native, vis_gpu_multifreq
     torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
