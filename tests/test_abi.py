@@ -109,3 +109,12 @@ def test_entry_points_reject_a_null_context(lib):
                                  4, 1, 0.3, None, None, None, None) == 1
     assert lib.hv_median_filter(None, None, None, 0, 0, 0, 3, 3) == 1
     assert lib.hv_median_filter_device(None, None, None, 0, 0, 0, 3, 3, None) == 1
+
+
+@pytest.mark.parametrize("std", ["c99", "c11"])
+def test_header_is_plain_c(tmp_path, std):
+    # the boundary is a C ABI: the header compiles as C, pedantic, warnings as errors
+    src = tmp_path / "use.c"
+    src.write_text('#include "heravis.h"\nint main(void) { hv_context* c = 0; (void)c; return 0; }\n')
+    subprocess.run(["gcc", f"-std={std}", "-Wall", "-Wextra", "-pedantic", "-Werror",
+                    "-fsyntax-only", "-I", os.path.join(ROOT, "include"), str(src)], check=True)
