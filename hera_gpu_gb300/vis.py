@@ -23,8 +23,10 @@ import numpy as np
 
 from . import _native
 
+ONE_OVER_C = 1.0 / 299792458.0   # s/m (vis.py:8); the library's delays use the same c
 NTHREADS = 1024          # reference module constants (vis.py:140-142), accepted only
 MAX_MEMORY = 2 ** 29
+MIN_CHUNK = 8
 
 
 def _resolve_precision(precision, real_dtype, complex_dtype):
