@@ -10,6 +10,7 @@ import pytest
 from scipy.interpolate import RectBivariateSpline
 
 from oracle import bilinear_beam, rel_frobenius, vis_oracle
+from oracle.vis_oracle import SPEED_OF_LIGHT, phasors
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 CASES = ["small_config", "random_inputs", "edge_inputs"]
@@ -92,3 +93,35 @@ def test_kat_two_sources():
     crd_eq[2, 1] = np.sqrt(0.5)
     v = vis_oracle(antpos, 1.0, eq2tops, crd_eq, np.ones(2), bm)
     np.testing.assert_almost_equal(v, 2, 2)
+
+
+# Known answers of the reference's kernel tests, restated on the oracle's
+# phasors (antennas at the origin, so v = A sqrt(I)).
+def test_kat_beam_interpolation_flat_and_middle():
+    # test_vis_gpu.py:31-65: a flat beam gives 1 above the horizon, 0 below
+    flat = np.ones((8, 31, 31))
+    crd = np.zeros((3, 128))
+    crd[2] = 0.9
+    args = (np.zeros((8, 3)), 150e6, np.identity(3))
+    np.testing.assert_array_equal(phasors(*args, crd, np.ones(128), flat), 1)
+    crd[2] = -0.9
+    np.testing.assert_array_equal(phasors(*args, crd, np.ones(128), flat), 0)
+    # test_vis_gpu.py:66-102: a beam of one centre pixel gives 1 at zenith,
+    # 0 at 45 degrees off it
+    middle = np.zeros((8, 31, 31))
+    middle[:, 15, 15] = 1.0
+    crd[:] = 0
+    crd[2] = 1.0
+    np.testing.assert_array_equal(phasors(*args, crd, np.ones(128), middle), 1)
+    crd[1] = crd[2] = 0.5 ** 0.5
+    np.testing.assert_array_equal(phasors(*args, crd, np.ones(128), middle), 0)
+
+
+def test_kat_whole_cycle_phase():
+    # test_vis_gpu.py:103-139: a delay of a whole number of cycles gives v = 1
+    freq = 150e6
+    antpos = np.zeros((2, 3))
+    antpos[1, 2] = 10 * SPEED_OF_LIGHT / freq        # ten wavelengths up
+    crd = np.array([[0.0], [0.0], [1.0]])
+    v = phasors(antpos, freq, np.identity(3), crd, np.ones(1), np.ones((2, 31, 31)))
+    np.testing.assert_allclose(v, 1, rtol=0, atol=1e-12)

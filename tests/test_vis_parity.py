@@ -95,6 +95,22 @@ def test_kat_values(method, precision):
 
 
 @pytest.mark.parametrize("method,precision", METHODS)
+def test_kat_beam_of_one_centre_pixel(method, precision):
+    # test_vis_gpu.py:66-102 through the whole call: a beam of one centre
+    # pixel gives A = 1 at zenith (V = the number of sources) and A = 0 at
+    # 45 degrees off it (V = 0)
+    antpos, eq2tops, crd_eq, I_sky, _ = kat_inputs()
+    middle = np.zeros((NANT, BM_PIX, BM_PIX))
+    middle[:, BM_PIX // 2, BM_PIX // 2] = 1.0
+    kw = dict(precision=precision, method=method)
+    v = vis_gpu(antpos, 1.0, eq2tops, crd_eq, I_sky, middle, **kw)
+    assert rel_frobenius(v, np.full(v.shape, NPIX, dtype=np.complex128)).max() <= \
+        TOL[(method, precision)]
+    crd_eq[1] = crd_eq[2] = np.sqrt(0.5)
+    np.testing.assert_equal(vis_gpu(antpos, 1.0, eq2tops, crd_eq, I_sky, middle, **kw), 0)
+
+
+@pytest.mark.parametrize("method,precision", METHODS)
 def test_dtypes_and_shapes(method, precision):
     # test_vis_gpu.py:172-202
     v = vis_gpu(np.zeros((NANT, 3)), 0.15, np.zeros((NTIMES, 3, 3)), np.zeros((3, NPIX)),
