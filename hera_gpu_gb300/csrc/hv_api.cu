@@ -180,6 +180,10 @@ int check_shapes(hv_context* ctx, int precision, int method, int nant, int nfreq
   if (nfreq < 1) return fail(ctx, HV_ERR_ARG, "nfreq must be >= 1 (got %d)", nfreq);
   if (ntimes < 0) return fail(ctx, HV_ERR_ARG, "ntimes must be >= 0 (got %d)", ntimes);
   if (nsrc < 0) return fail(ctx, HV_ERR_ARG, "nsrc must be >= 0 (got %d)", nsrc);
+  // (time, frequency) slices are counted in int by the kernels
+  if ((long long)ntimes * nfreq > 0x7fffffffLL)
+    return fail(ctx, HV_ERR_ARG, "ntimes x nfreq = %lld slices exceeds 2^31 - 1",
+                (long long)ntimes * nfreq);
   if (P < 1 || P > 4096) return fail(ctx, HV_ERR_ARG, "beam_px must be in [1, 4096] (got %d)", P);
   return HV_OK;
 }

@@ -28,6 +28,8 @@
  *      vis     (ntimes, nant, nant) output
  *    Multi-frequency calls take bm_cubes (nfreq, nant, P, P) and write
  *    vis (nfreq, ntimes, nant, nant).
+ *  - Limits (HV_ERR_ARG beyond them): 1 <= nant <= 65536, 1 <= P <= 4096,
+ *    ntimes x nfreq <= 2^31 - 1.
  *  - A context owns one CUDA stream and a workspace on one device; it is not
  *    thread-safe (one thread per context, or a lock around it).
  */
