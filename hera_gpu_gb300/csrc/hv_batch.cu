@@ -311,7 +311,7 @@ int enqueue(hv_batch* b, cudaStream_t st, int timed_class = -1) {
 
 int check_sim(hv_batch* b, const hv_sim& s, int i) {
   if (s.nant < 1 || s.nant > 65536 || s.ntimes < 0 || s.nsrc < 0 || s.nfreq < 1 ||
-      s.beam_px < 1 || s.beam_px > 4096)
+      s.beam_px < 1 || s.beam_px > 4096 || (long long)s.ntimes * s.nfreq > 0x7fffffffLL)
     return bfail(b, HV_ERR_ARG, "simulation %d: bad sizes (nant %d ntimes %d nsrc %d nfreq %d P %d)",
                  i, s.nant, s.ntimes, s.nsrc, s.nfreq, s.beam_px);
   if (!s.antpos || !s.eq2tops || !s.bm_cubes || !s.freqs || !s.vis_out ||
