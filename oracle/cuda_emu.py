@@ -4,12 +4,21 @@ INFRASTRUCTURE ONLY (used by oracle/redcal_ref.py and oracle/median_ref.py).
 The reference compiles its kernels at run time from source strings
 (pycuda SourceModule).  Here such a string is compiled with g++ behind a
 prelude that defines the CUDA built-ins for the host -- blockIdx, threadIdx,
-blockDim and gridDim as globals, atomicAdd as a plain addition,
-__syncthreads as nothing, __shared__ arrays and __global__ / __device__
-functions as static ones, the integer min / max, and an empty ``texture``
-template -- into oracle/_ref/.  A launch runs every
-thread of the grid in turn: blocks y-major, then the threads of a block
-y-major.  The source is compiled as given; nothing of it is rewritten.
+blockDim and gridDim, __shared__ arrays and __global__ / __device__
+functions as static ones, the integer min / max, and textures (a
+``texture`` object holds a host array set through ``get_texref(name)
+.set_array``; ``fp_tex3D`` is an unnormalised, point-sampled, clamped fetch,
+the reference's texture set-up) -- into oracle/_ref/.  The source is
+compiled as given; nothing of it is rewritten.  Two ways to run a launch:
+
+* sequential (default): every thread of the grid in turn, blocks y-major,
+  then the threads of a block y-major; __syncthreads is nothing and
+  atomicAdd a plain addition.  Right for kernels whose barriers only order
+  writes before reads of later threads in that order.
+* threaded: one block at a time, each of its threads an OS thread;
+  __syncthreads is a barrier that a returned thread leaves, atomicAdd an
+  atomic addition.  Right for any kernel whose threads exchange data
+  through shared memory in both directions.
 """
 from __future__ import annotations
 
@@ -28,23 +37,79 @@ CUDA_INCLUDE = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "inc
 PRELUDE = r"""
 #include <cmath>
 #include <cstdio>
+#include <cstddef>
+#include <texture_types.h>
 %(includes)s
 #undef __global__
 #undef __device__
 #define __global__ static
 #define __device__ static
-template <typename T, int D> struct texture {};
 typedef unsigned int uint;
 struct EmuDim3 { unsigned x, y, z; };
-static EmuDim3 blockIdx, threadIdx, blockDim, gridDim;
-#define __syncthreads()
+static EmuDim3 blockIdx, blockDim, gridDim;
 #define __shared__ static
 static inline int min(int a, int b) { return a < b ? a : b; }
 static inline int max(int a, int b) { return a > b ? a : b; }
 static inline unsigned min(unsigned a, unsigned b) { return a < b ? a : b; }
 static inline unsigned max(unsigned a, unsigned b) { return a > b ? a : b; }
+template <typename T, int D = 1, int M = 0> struct texture {
+  const T* data = nullptr;
+  int w = 0, h = 0, d = 0;
+};
+typedef float fp_tex_float;
+typedef double fp_tex_double;
+static inline long emu_texel(double c, int n) {
+  long i = (long)std::floor(c);
+  return i < 0 ? 0 : (i >= n ? n - 1 : i);
+}
+template <typename T, int D, int M>
+static inline T fp_tex3D(const texture<T, D, M>& t, double x, double y, double z) {
+  return t.data[(emu_texel(z, t.d) * t.h + emu_texel(y, t.h)) * t.w + emu_texel(x, t.w)];
+}
+%(mode)s
+"""
+
+SEQUENTIAL = r"""
+static EmuDim3 threadIdx;
+#define __syncthreads()
 static inline float atomicAdd(float* a, float v) { float o = *a; *a = o + v; return o; }
 static inline double atomicAdd(double* a, double v) { double o = *a; *a = o + v; return o; }
+"""
+
+THREADED = r"""
+#include <condition_variable>
+#include <mutex>
+#include <thread>
+#include <vector>
+static thread_local EmuDim3 threadIdx;
+// __syncthreads: every thread of the block that has not returned arrives;
+// a thread that returns leaves the barrier (arrive_and_drop)
+struct EmuBarrier {
+  std::mutex m;
+  std::condition_variable cv;
+  long expected, waiting = 0, phase = 0;
+  explicit EmuBarrier(long n) : expected(n) {}
+  void release() { waiting = 0; ++phase; cv.notify_all(); }
+  void arrive_and_wait() {
+    std::unique_lock<std::mutex> lock(m);
+    const long ph = phase;
+    if (++waiting == expected) { release(); return; }
+    cv.wait(lock, [&] { return phase != ph; });
+  }
+  void arrive_and_drop() {
+    std::lock_guard<std::mutex> lock(m);
+    if (--expected > 0 && waiting == expected) release();
+  }
+};
+static EmuBarrier* emu_bar;
+#define __syncthreads() emu_bar->arrive_and_wait()
+static std::mutex emu_atomic_mu;
+static inline float atomicAdd(float* a, float v) {
+  std::lock_guard<std::mutex> lock(emu_atomic_mu); float o = *a; *a = o + v; return o;
+}
+static inline double atomicAdd(double* a, double v) {
+  std::lock_guard<std::mutex> lock(emu_atomic_mu); double o = *a; *a = o + v; return o;
+}
 """
 
 _SCALAR = {"uint": ctypes.c_uint, "int": ctypes.c_int, "float": ctypes.c_float,
@@ -64,6 +129,11 @@ def parse_kernels(code):
             ps.append((None if "*" in ptype else ptype, ptype, pname))
         out.append((name, ps))
     return out
+
+
+def parse_textures(code):
+    """Names of the file-scope ``texture<...> name;`` declarations."""
+    return re.findall(r"texture\s*<[^;{}]*>\s*(\w+)\s*;", code)
 
 
 def _address(a):
@@ -100,11 +170,53 @@ class Kernel:
         self(*args, block=block, grid=grid)
 
 
-class Module:
-    """The kernels of one source string, compiled for the host."""
+class _TexRef:
+    """A texture of the module: ``set_array`` points it at a host array of
+    shape (depth, height, width), which it keeps alive."""
 
-    def __init__(self, code, includes="", defines=""):
+    def __init__(self, setter):
+        self.setter, self.array = setter, None
+
+    def set_array(self, array):
+        a = np.ascontiguousarray(array.arr if hasattr(array, "arr") else array)
+        d, h, w = (1,) * (3 - a.ndim) + a.shape
+        self.array = a
+        self.setter(ctypes.c_void_p(a.ctypes.data), w, h, d)
+
+
+_SEQUENTIAL_LAUNCH = (
+    "  for (unsigned y = 0; y < gy; ++y) for (unsigned x = 0; x < gx; ++x) {{\n"
+    "    blockIdx = {{x, y, 0u}};\n"
+    "    for (unsigned tz = 0; tz < tbz; ++tz) for (unsigned ty = 0; ty < tby; ++ty)\n"
+    "      for (unsigned tx = 0; tx < tbx; ++tx) {{\n"
+    "        threadIdx = {{tx, ty, tz}}; {name}({call});\n"
+    "      }}\n  }}\n")
+
+_THREADED_LAUNCH = (
+    "  const long nth = (long)tbx * tby * tbz;\n"
+    "  for (unsigned y = 0; y < gy; ++y) for (unsigned x = 0; x < gx; ++x) {{\n"
+    "    blockIdx = {{x, y, 0u}};\n"
+    "    EmuBarrier bar(nth);\n"
+    "    emu_bar = &bar;\n"
+    "    std::vector<std::thread> ts;\n"
+    "    ts.reserve((size_t)nth);\n"
+    "    for (unsigned tz = 0; tz < tbz; ++tz) for (unsigned ty = 0; ty < tby; ++ty)\n"
+    "      for (unsigned tx = 0; tx < tbx; ++tx)\n"
+    "        ts.emplace_back([&, tx, ty, tz] {{\n"
+    "          threadIdx = {{tx, ty, tz}}; {name}({call}); bar.arrive_and_drop();\n"
+    "        }});\n"
+    "    for (auto& t : ts) t.join();\n"
+    "  }}\n")
+
+
+class Module:
+    """The kernels of one source string, compiled for the host; ``threaded``
+    picks how a launch runs its threads (see the module docstring)."""
+
+    def __init__(self, code, includes="", defines="", threaded=False):
         kernels = parse_kernels(code)
+        textures = parse_textures(code)
+        launch = _THREADED_LAUNCH if threaded else _SEQUENTIAL_LAUNCH
         wrappers = []
         for name, ps in kernels:
             decl = ", ".join(f"{t} {n}" for _, t, n in ps)
@@ -113,13 +225,15 @@ class Module:
                 f'extern "C" void emu_{name}(unsigned gx, unsigned gy, unsigned tbx, unsigned tby, '
                 f"unsigned tbz{', ' if decl else ''}{decl}) {{\n"
                 "  gridDim = {gx, gy, 1u}; blockDim = {tbx, tby, tbz};\n"
-                "  for (unsigned y = 0; y < gy; ++y) for (unsigned x = 0; x < gx; ++x) {\n"
-                "    blockIdx = {x, y, 0u};\n"
-                "    for (unsigned tz = 0; tz < tbz; ++tz) for (unsigned ty = 0; ty < tby; ++ty)\n"
-                "      for (unsigned tx = 0; tx < tbx; ++tx) {\n"
-                f"        threadIdx = {{tx, ty, tz}}; {name}({call});\n"
-                "      }\n  }\n}\n")
-        src = defines + PRELUDE % {"includes": includes} + code + "\n" + "".join(wrappers)
+                + launch.format(name=name, call=call) + "}\n")
+        for t in textures:
+            wrappers.append(
+                f'extern "C" void emu_settex_{t}(const void* p, int w, int h, int d) {{\n'
+                f"  {t}.data = static_cast<decltype({t}.data)>(p); {t}.w = w; {t}.h = h; "
+                f"{t}.d = d;\n}}\n")
+        src = defines + PRELUDE % {"includes": includes,
+                                   "mode": THREADED if threaded else SEQUENTIAL} + \
+            code + "\n" + "".join(wrappers)
         key = hashlib.sha256(src.encode()).hexdigest()[:16]
         os.makedirs(OUT, exist_ok=True)
         inc = os.path.join(OUT, "include")
@@ -129,13 +243,19 @@ class Module:
         if not os.path.exists(so):
             cpp = so[:-3] + ".cpp"
             open(cpp, "w").write(src)
-            subprocess.run(["g++", "-O2", "-shared", "-fPIC", "-w", "-I", CUDA_INCLUDE, "-I", inc,
-                            cpp, "-o", so], check=True)
+            subprocess.run(["g++", "-std=c++17", "-O2", "-shared", "-fPIC", "-pthread", "-w",
+                            "-I", CUDA_INCLUDE, "-I", inc, cpp, "-o", so], check=True)
         lib = ctypes.CDLL(so)
         self.kernels = {name: Kernel(getattr(lib, f"emu_{name}"), ps) for name, ps in kernels}
+        self.textures = {}
+        for t in textures:
+            setter = getattr(lib, f"emu_settex_{t}")
+            setter.restype = None
+            setter.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+            self.textures[t] = _TexRef(setter)
 
     def get_function(self, name):
         return self.kernels[name]
 
     def get_texref(self, name):
-        return None
+        return self.textures[name]

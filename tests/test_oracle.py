@@ -1,7 +1,9 @@
 """The oracle against the reference's own outputs and known answers (CPU).
 
 The fixtures under tests/golden/ were produced by running the reference's
-``vis_cpu`` (hera_gpu/tests/test_vis_gpu.py:278-357); see make_golden.py.
+``vis_cpu`` (hera_gpu/tests/test_vis_gpu.py:278-357; make_golden.py) and the
+reference's ``vis_gpu`` itself -- its host loop and kernels, run on the CPU
+(hera_gpu/vis.py:144-262; make_vis_gpu_golden.py) -- on the same inputs.
 """
 import os
 
@@ -11,6 +13,7 @@ from scipy.interpolate import RectBivariateSpline
 
 from oracle import bilinear_beam, rel_frobenius, vis_oracle
 from oracle.vis_oracle import SPEED_OF_LIGHT, phasors
+from vis_gpu_cases import VIS_GPU_CASES, load_vis_gpu_case
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 CASES = ["small_config", "random_inputs", "edge_inputs"]
@@ -125,3 +128,28 @@ def test_kat_whole_cycle_phase():
     crd = np.array([[0.0], [0.0], [1.0]])
     v = phasors(antpos, freq, np.identity(3), crd, np.ones(1), np.ones((2, 31, 31)))
     np.testing.assert_allclose(v, 1, rtol=0, atol=1e-12)
+
+
+def as_f32(x):
+    return np.asarray(x).astype(np.float32).astype(np.float64)
+
+
+@pytest.mark.parametrize("name", VIS_GPU_CASES)
+def test_oracle_matches_the_reference_vis_gpu(name):
+    used, _, out = load_vis_gpu_case(name)
+    # FP64: the reference's vis_gpu and the oracle agree to rounding
+    # (measured <= 3e-16, sources past the beam grid's edge included)
+    assert rel_frobenius(out[2], vis_oracle(*used)).max() < 1e-13
+    # FP32: the reference's own error, on the inputs as it sees them; its
+    # delays come from an FP32 GEMM, so km baselines (edge_inputs) carry 3.5e-4
+    a, f, e, s, i, b = used
+    ref32 = vis_oracle(as_f32(a), f, as_f32(e), as_f32(s), as_f32(i), as_f32(b))
+    bound = 1e-3 if name == "edge_inputs" else 1e-5
+    assert rel_frobenius(out[1], ref32).max() < bound
+
+
+def test_reference_vis_gpu_drops_the_remainder_sources():
+    # vis.py:176-177: 1003 sources in 8 chunks of 125; the last 3 are not summed
+    used, full, out = load_vis_gpu_case("ragged")
+    assert used[3].shape[1] == 1000 and full[3].shape[1] == 1003
+    assert rel_frobenius(out[2], vis_oracle(*full)).max() > 1e-4

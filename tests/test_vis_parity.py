@@ -15,6 +15,7 @@ import pytest
 
 from hera_gpu_gb300 import synth, vis_gpu, vis_gpu_multifreq
 from oracle import rel_frobenius, vis_oracle
+from vis_gpu_cases import VIS_GPU_CASES, load_vis_gpu_case
 
 pytestmark = pytest.mark.gpu
 
@@ -56,6 +57,17 @@ def test_golden_fixtures(name, method, precision):
     # Hermitian with a real diagonal, as the reference's mirror step leaves it
     np.testing.assert_array_equal(v, np.conj(np.transpose(v, (0, 2, 1))))
     assert np.all(np.diagonal(v, axis1=1, axis2=2).imag == 0)
+
+
+@pytest.mark.parametrize("method,precision", METHODS)
+@pytest.mark.parametrize("name", VIS_GPU_CASES)
+def test_reference_vis_gpu_fixtures(name, method, precision):
+    # the reference's own vis_gpu (run on the CPU) on the sources it sums
+    used, _, out = load_vis_gpu_case(name)
+    v = vis_gpu(*used, precision=precision, method=method)
+    assert rel_frobenius(v, oracle_same_inputs(used, precision)).max() <= TOL[(method, precision)]
+    if precision == 2:
+        assert rel_frobenius(v, out[2]).max() < 1e-11
 
 
 # --- known answers of test_vis_gpu.py:203-244 -------------------------------
