@@ -10,7 +10,6 @@ fails only its own requests while the loop keeps serving.
 import types
 
 import numpy as np
-import pytest
 
 from hera_gpu_gb300 import _native, serve
 
