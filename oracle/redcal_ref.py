@@ -100,7 +100,9 @@ def _stubs():
     hera_cal.redcal = hc_redcal
     mods["hera_cal"], mods["hera_cal.redcal"] = hera_cal, hc_redcal
     linsolve = types.ModuleType("linsolve")
-    linsolve.get_name = lambda s: s
+    # linsolve's rule: a trailing '_' marks a conjugated variable and is
+    # not part of its name
+    linsolve.get_name = lambda s: s.rstrip("_") if isinstance(s, str) else str(s)
     mods["linsolve"] = linsolve
     clash = [k for k in mods if k in sys.modules]
     assert not clash, f"real modules present: {clash}"
@@ -122,3 +124,29 @@ def reference_omnical(ref_root, *args, **kwargs):
         mod = importlib.util.module_from_spec(spec)
         spec.loader.exec_module(mod)
         return mod.omnical(*args, **kwargs)
+
+
+def reference_solve_iteratively(ref_root, attrs, **kwargs):
+    """The reference's ``OmnicalSolverGPU.solve_iteratively``
+    (redcal.py:747-837) on an OmnicalSolverGPU whose attributes are
+    ``attrs`` (sol0, all_terms, keys, data, wgts, gain), the reference's own
+    code on the CPU.  Returns (meta, sol, calls): ``calls`` records the
+    arguments and the result of every ``omnical`` call it made."""
+    calls = []
+    with _stubs():
+        path = os.path.join(ref_root, "hera_gpu", "redcal.py")
+        spec = importlib.util.spec_from_file_location("_reference_redcal", path)
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        inner = mod.omnical
+
+        def recording(*args, **kw):
+            out = inner(*args, **kw)
+            calls.append({"args": args, "kwargs": kw, "result": out})
+            return out
+
+        mod.omnical = recording
+        solver = mod.OmnicalSolverGPU()
+        solver.__dict__.update(attrs)
+        meta, sol = solver.solve_iteratively(**kwargs)
+    return meta, sol, calls

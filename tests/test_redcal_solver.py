@@ -5,10 +5,15 @@ CPU: packing a solver's equations and starting solution into ``omnical``'s
 arrays (names numbered in first-appearance order, conjugation marks
 dropped), unpacking a result by name into the solution's shape, and the two
 classes made on hera_cal's -- with a stand-in ``hera_cal.redcal`` module and
-a stand-in ``omnical`` that records its arguments.  GPU: the solver path
+a stand-in ``omnical`` that records its arguments.  Pinned to the
+reference's own solve_iteratively run on the CPU
+(tests/golden/make_redcal_solver_golden.py): the same arrays handed to
+``omnical``, and from the same ``omnical`` result the same meta and
+solution, types included.  GPU: the solver path
 against ``omnical`` on the same arrays (the same launch, so equal) and
 against the oracle, on a 19-antenna hexagonal array in float64.
 """
+import os
 import sys
 import types
 
@@ -17,31 +22,9 @@ import pytest
 
 from hera_gpu_gb300 import redcal, synth
 from oracle import omnical_oracle
+from solver_cases import FakeSolver, gain_name, ubl_name
 
 SHAPE = (6, 4)       # (times, frequencies): 24 problems
-
-
-def gain_name(a):
-    return f"g_{a}_Jxx"
-
-
-def ubl_name(k):
-    return f"u_{k}_xx"
-
-
-class FakeSolver:
-    """The attributes of hera_cal's OmnicalSolver that the packing reads:
-    one product term g_i * conj(g_j) * u_k per data key, the conjugated
-    factor named with linsolve's trailing '_'."""
-
-    def __init__(self, ggu, gains, ubls, data, wgts, shape, gain=0.3):
-        self.keys = [(int(i), int(j), "xx") for i, j, _ in ggu]
-        self.all_terms = [[(gain_name(i), gain_name(j) + "_", ubl_name(k))] for i, j, k in ggu]
-        self.sol0 = {gain_name(a): gains[:, a].reshape(shape) for a in range(gains.shape[1])}
-        self.sol0.update({ubl_name(k): ubls[:, k].reshape(shape) for k in range(ubls.shape[1])})
-        self.data = {key: data[:, b].reshape(shape) for b, key in enumerate(self.keys)}
-        self.wgts = {key: wgts[:, b].reshape(shape) for b, key in enumerate(self.keys)}
-        self.gain = gain
 
 
 def hex_solver(dtype=np.complex128, seed=3, gain=0.3):
@@ -199,6 +182,56 @@ def test_omnical_gpu_keys_and_arguments(stand_in_hera_cal, monkeypatch):
     assert (fake.args["conv_crit"], fake.args["maxiter"], fake.args["check_every"],
             fake.args["check_after"], fake.args["precision"]) == (1e-12, 500, 6, 30, 1)
     assert meta["iter"].shape == SHAPE
+
+
+REFERENCE = os.path.join(os.path.dirname(__file__), "golden", "redcal_solver_reference.npz")
+REFERENCE_CASES = ["c64_auto", "c128_auto", "c128_p1"]
+
+
+def reference_case(case):
+    """The reference's own solve_iteratively on a 19-antenna hex array of
+    3 x 2 problems (tests/golden/make_redcal_solver_golden.py): the solver
+    it ran on, its precision argument and what it did."""
+    z = np.load(REFERENCE)
+    ggu, _ = synth.hex_redundant_layout(19)
+    solver = FakeSolver(ggu, z[f"{case}_in_g0"], z[f"{case}_in_u0"], z[f"{case}_in_d"],
+                        z[f"{case}_in_w"], (3, 2), 0.3)
+    p = int(z[f"{case}_precision"])
+    return z, solver, (None if p < 0 else p)
+
+
+@pytest.mark.parametrize("case", REFERENCE_CASES)
+def test_pack_solver_matches_the_reference(case):
+    # the arrays the reference's solve_iteratively handed to its omnical
+    z, solver, precision = reference_case(case)
+    p = redcal.pack_solver(solver, precision)
+    np.testing.assert_array_equal(p["ggu"].astype(np.int64),
+                                  z[f"{case}_omnical_ggu"].astype(np.int64))
+    for k in ("gains", "ubls", "data", "wgts"):
+        ref = z[f"{case}_omnical_{k}"]
+        assert p[k].dtype == ref.dtype, k
+        np.testing.assert_array_equal(p[k], ref)
+    assert p["precision"] == int(z[f"{case}_omnical_precision"])
+    assert solver.gain == float(z[f"{case}_omnical_gain"])
+
+
+@pytest.mark.parametrize("case", REFERENCE_CASES)
+def test_solve_iteratively_matches_the_reference(case, monkeypatch):
+    # given what the reference's omnical returned, the same meta and solution
+    z, solver, precision = reference_case(case)
+    result = {k: z[f"{case}_result_{k}"].copy() for k in ("gains", "ubls", "chisq", "iters", "conv")}
+    monkeypatch.setattr(redcal, "omnical", lambda *args, **kwargs: result)
+    meta, sol = redcal.solve_iteratively(solver, conv_crit=1e-10, maxiter=60,
+                                         precision=precision)
+    for k in ("iter", "chisq", "conv_crit"):
+        ref = z[f"{case}_meta_{k}"]
+        assert meta[k].dtype == ref.dtype, k
+        np.testing.assert_array_equal(meta[k], ref)
+    names = [str(n) for n in z[f"{case}_sol_names"]]
+    assert sorted(sol) == names
+    for name, value in zip(names, z[f"{case}_sol_values"]):
+        np.testing.assert_array_equal(sol[name], value)
+        assert sol[name].shape == value.shape and sol[name].dtype == value.dtype
 
 
 # ---------------------------------------------------------------- GPU
