@@ -6,8 +6,10 @@ GPU, to produce reference outputs for tests/golden/ (make_omnical_golden.py):
 
 * the reference's imports are stubbed: pycuda arrays are numpy arrays
   (zero-filled, where pycuda's gpuarray.empty leaves memory as it finds it),
-  events are no-ops, the two cuBLAS copies are memory copies, and the
-  hera_cal / linsolve names its wrapper classes use are placeholders;
+  events are no-ops, the two cuBLAS copies are memory copies, hera_cal's
+  OmnicalSolver / RedundantCalibrator are empty base classes, and
+  linsolve's get_name is its rule (a trailing '_' marks a conjugated
+  variable and is not part of the name);
 * ``SourceModule`` is oracle/cuda_emu.py: the kernel source exactly as the
   reference formats it, compiled with g++ for the host, a launch run as a
   loop over every thread -- blocks y-major, then threads y-major, so that in
@@ -16,8 +18,11 @@ GPU, to produce reference outputs for tests/golden/ (make_omnical_golden.py):
   orders them.
 
 The atomic sums are thus taken in thread order, which the GPU does not fix;
-their rounding differs from any one GPU run at the last bits.  Needs the
-reference sources; the tests use the fixtures it made.
+their rounding differs from any one GPU run at the last bits.
+``reference_solve_iteratively`` runs the reference's
+``OmnicalSolverGPU.solve_iteratively`` (redcal.py:747-837) the same way, for
+tests/golden/make_redcal_solver_golden.py.  Needs the reference sources; the
+tests use the fixtures it made.
 """
 from __future__ import annotations
 
