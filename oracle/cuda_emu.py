@@ -15,10 +15,13 @@ compiled as given; nothing of it is rewritten.  Two ways to run a launch:
   then the threads of a block y-major; __syncthreads is nothing and
   atomicAdd a plain addition.  Right for kernels whose barriers only order
   writes before reads of later threads in that order.
-* threaded: one block at a time, each of its threads an OS thread;
-  __syncthreads is a barrier that a returned thread leaves, atomicAdd an
-  atomic addition.  Right for any kernel whose threads exchange data
-  through shared memory in both directions.
+* barriers: one block at a time, each of its threads a fiber (ucontext)
+  on the calling thread; __syncthreads returns to the block's scheduler,
+  which runs every thread that has not returned up to its next barrier
+  before any goes past it -- CUDA's barrier semantics, deterministic.
+  atomicAdd is a plain addition (one thread at a time).  Right for any
+  kernel whose threads exchange data through shared memory in both
+  directions.
 """
 from __future__ import annotations
 
@@ -76,40 +79,53 @@ static inline float atomicAdd(float* a, float v) { float o = *a; *a = o + v; ret
 static inline double atomicAdd(double* a, double v) { double o = *a; *a = o + v; return o; }
 """
 
-THREADED = r"""
-#include <condition_variable>
-#include <mutex>
-#include <thread>
+BARRIERS = r"""
+#include <ucontext.h>
+#include <functional>
 #include <vector>
-static thread_local EmuDim3 threadIdx;
-// __syncthreads: every thread of the block that has not returned arrives;
-// a thread that returns leaves the barrier (arrive_and_drop)
-struct EmuBarrier {
-  std::mutex m;
-  std::condition_variable cv;
-  long expected, waiting = 0, phase = 0;
-  explicit EmuBarrier(long n) : expected(n) {}
-  void release() { waiting = 0; ++phase; cv.notify_all(); }
-  void arrive_and_wait() {
-    std::unique_lock<std::mutex> lock(m);
-    const long ph = phase;
-    if (++waiting == expected) { release(); return; }
-    cv.wait(lock, [&] { return phase != ph; });
-  }
-  void arrive_and_drop() {
-    std::lock_guard<std::mutex> lock(m);
-    if (--expected > 0 && waiting == expected) release();
-  }
+static EmuDim3 threadIdx;
+// Each thread of a block is a fiber (ucontext) on this one OS thread; a
+// barrier hands control back to the block's scheduler, which runs every
+// live fiber up to its next barrier (or its return) before any goes on.
+struct EmuFiber {
+  ucontext_t ctx;
+  unsigned tx, ty, tz;
+  bool done;
 };
-static EmuBarrier* emu_bar;
-#define __syncthreads() emu_bar->arrive_and_wait()
-static std::mutex emu_atomic_mu;
-static inline float atomicAdd(float* a, float v) {
-  std::lock_guard<std::mutex> lock(emu_atomic_mu); float o = *a; *a = o + v; return o;
+static ucontext_t emu_main;
+static EmuFiber* emu_cur;
+static std::function<void()> emu_body;
+static void emu_entry() { emu_body(); emu_cur->done = true; }
+#define __syncthreads() swapcontext(&emu_cur->ctx, &emu_main)
+static void emu_run_block(long nth, unsigned tbx, unsigned tby, std::function<void()> body) {
+  const size_t stack = 256 * 1024;
+  static std::vector<char> stacks;
+  if (stacks.size() < stack * nth) stacks.resize(stack * nth);
+  std::vector<EmuFiber> fib((size_t)nth);
+  emu_body = std::move(body);
+  for (long t = 0; t < nth; ++t) {
+    EmuFiber& f = fib[(size_t)t];
+    f.tx = (unsigned)(t % tbx); f.ty = (unsigned)(t / tbx % tby); f.tz = (unsigned)(t / tbx / tby);
+    f.done = false;
+    getcontext(&f.ctx);
+    f.ctx.uc_stack.ss_sp = stacks.data() + stack * (size_t)t;
+    f.ctx.uc_stack.ss_size = stack;
+    f.ctx.uc_link = &emu_main;
+    makecontext(&f.ctx, emu_entry, 0);
+  }
+  for (bool live = true; live;) {
+    live = false;
+    for (EmuFiber& f : fib) {
+      if (f.done) continue;
+      emu_cur = &f;
+      threadIdx = {f.tx, f.ty, f.tz};
+      swapcontext(&emu_main, &f.ctx);
+      live |= !f.done;
+    }
+  }
 }
-static inline double atomicAdd(double* a, double v) {
-  std::lock_guard<std::mutex> lock(emu_atomic_mu); double o = *a; *a = o + v; return o;
-}
+static inline float atomicAdd(float* a, float v) { float o = *a; *a = o + v; return o; }
+static inline double atomicAdd(double* a, double v) { double o = *a; *a = o + v; return o; }
 """
 
 _SCALAR = {"uint": ctypes.c_uint, "int": ctypes.c_int, "float": ctypes.c_float,
@@ -192,31 +208,22 @@ _SEQUENTIAL_LAUNCH = (
     "        threadIdx = {{tx, ty, tz}}; {name}({call});\n"
     "      }}\n  }}\n")
 
-_THREADED_LAUNCH = (
+_BARRIER_LAUNCH = (
     "  const long nth = (long)tbx * tby * tbz;\n"
     "  for (unsigned y = 0; y < gy; ++y) for (unsigned x = 0; x < gx; ++x) {{\n"
     "    blockIdx = {{x, y, 0u}};\n"
-    "    EmuBarrier bar(nth);\n"
-    "    emu_bar = &bar;\n"
-    "    std::vector<std::thread> ts;\n"
-    "    ts.reserve((size_t)nth);\n"
-    "    for (unsigned tz = 0; tz < tbz; ++tz) for (unsigned ty = 0; ty < tby; ++ty)\n"
-    "      for (unsigned tx = 0; tx < tbx; ++tx)\n"
-    "        ts.emplace_back([&, tx, ty, tz] {{\n"
-    "          threadIdx = {{tx, ty, tz}}; {name}({call}); bar.arrive_and_drop();\n"
-    "        }});\n"
-    "    for (auto& t : ts) t.join();\n"
+    "    emu_run_block(nth, tbx, tby, [&] {{ {name}({call}); }});\n"
     "  }}\n")
 
 
 class Module:
-    """The kernels of one source string, compiled for the host; ``threaded``
+    """The kernels of one source string, compiled for the host; ``barriers``
     picks how a launch runs its threads (see the module docstring)."""
 
-    def __init__(self, code, includes="", defines="", threaded=False):
+    def __init__(self, code, includes="", defines="", barriers=False):
         kernels = parse_kernels(code)
         textures = parse_textures(code)
-        launch = _THREADED_LAUNCH if threaded else _SEQUENTIAL_LAUNCH
+        launch = _BARRIER_LAUNCH if barriers else _SEQUENTIAL_LAUNCH
         wrappers = []
         for name, ps in kernels:
             decl = ", ".join(f"{t} {n}" for _, t, n in ps)
@@ -232,7 +239,7 @@ class Module:
                 f"  {t}.data = static_cast<decltype({t}.data)>(p); {t}.w = w; {t}.h = h; "
                 f"{t}.d = d;\n}}\n")
         src = defines + PRELUDE % {"includes": includes,
-                                   "mode": THREADED if threaded else SEQUENTIAL} + \
+                                   "mode": BARRIERS if barriers else SEQUENTIAL} + \
             code + "\n" + "".join(wrappers)
         key = hashlib.sha256(src.encode()).hexdigest()[:16]
         os.makedirs(OUT, exist_ok=True)
@@ -243,7 +250,7 @@ class Module:
         if not os.path.exists(so):
             cpp = so[:-3] + ".cpp"
             open(cpp, "w").write(src)
-            subprocess.run(["g++", "-std=c++17", "-O2", "-shared", "-fPIC", "-pthread", "-w",
+            subprocess.run(["g++", "-std=c++17", "-O2", "-shared", "-fPIC", "-w",
                             "-I", CUDA_INCLUDE, "-I", inc, cpp, "-o", so], check=True)
         lib = ctypes.CDLL(so)
         self.kernels = {name: Kernel(getattr(lib, f"emu_{name}"), ps) for name, ps in kernels}

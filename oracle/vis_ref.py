@@ -6,12 +6,12 @@ its stream loop and its host-side sum) and its two CUDA kernels,
 without a GPU, to produce reference outputs for tests/golden/
 (make_vis_gpu_golden.py):
 
-* ``SourceModule`` is oracle/cuda_emu.py in its threaded mode: the kernel
-  source exactly as the reference formats it, compiled with g++ for the
-  host, each block's threads run as OS threads with a real barrier, since
-  InterpolateBeam's threads exchange beam coordinates through shared memory
-  in both directions.  CUDA's float overloads of cos / sin / fma are the C++
-  library's float overloads.
+* ``SourceModule`` is oracle/cuda_emu.py with barriers: the kernel source
+  exactly as the reference formats it, compiled with g++ for the host, each
+  block's threads run as fibers that all reach a barrier before any passes
+  it, since InterpolateBeam's threads exchange beam coordinates through
+  shared memory in both directions.  CUDA's float overloads of cos / sin /
+  fma are the C++ library's float overloads.
 * The beam texture is a host array read by point-sampled, clamped fetches
   at unnormalised coordinates -- the reference's texture set-up
   (vis.py:113-138: an array of (nant, P, P), no filtering, default address
@@ -103,7 +103,7 @@ class _Memcpy3D(_Bag):
 
 
 def _source_module(code):
-    return cuda_emu.Module(code, includes=_INCLUDES, threaded=True)
+    return cuda_emu.Module(code, includes=_INCLUDES, barriers=True)
 
 
 def _gemm(dtype):

@@ -1,6 +1,6 @@
 """oracle/cuda_emu.py, the host emulation that runs the reference's CUDA
-kernel strings for the parity fixtures: its two launch modes, barriers that
-threads leave by returning, atomics, and texture fetches.  CPU only (g++)."""
+kernel strings for the parity fixtures: its two launch modes, barriers past
+threads that returned, atomics, and texture fetches.  CPU only (g++)."""
 import numpy as np
 import pytest
 
@@ -47,10 +47,10 @@ __global__ void fetch(const float* xyz, float* out, int n)
 """
 
 
-def test_threaded_mode_orders_shared_memory_through_the_barrier():
+def test_barriers_order_shared_memory_both_ways():
     n = 100
     out = np.zeros(n, dtype=np.float32)
-    cuda_emu.Module(REVERSE, threaded=True).get_function("reverse")(
+    cuda_emu.Module(REVERSE, barriers=True).get_function("reverse")(
         out, np.int32(n), block=(32, 1, 1), grid=(4, 1))
     want = np.empty(n, dtype=np.float32)
     for i in range(n):
@@ -76,17 +76,17 @@ def test_returned_threads_leave_the_barrier_and_atomics_add():
     x = np.arange(1, n + 1, dtype=np.float32)
     out = np.zeros(3, dtype=np.float32)
     total = np.zeros(1, dtype=np.float32)
-    cuda_emu.Module(EARLY, threaded=True).get_function("partial_sums")(
+    cuda_emu.Module(EARLY, barriers=True).get_function("partial_sums")(
         x, out, total, np.int32(n), block=(32, 1, 1), grid=(3, 1))
     np.testing.assert_array_equal(out, [x[:32].sum(), x[32:64].sum(), x[64:].sum()])
     assert total[0] == x.sum()
 
 
-@pytest.mark.parametrize("threaded", [False, True])
-def test_texture_fetch_is_point_sampled_and_clamped(threaded):
+@pytest.mark.parametrize("barriers", [False, True])
+def test_texture_fetch_is_point_sampled_and_clamped(barriers):
     d, h, w = 2, 3, 4
     arr = np.arange(d * h * w, dtype=np.float32).reshape(d, h, w)
-    mod = cuda_emu.Module(TEXTURE, threaded=threaded)
+    mod = cuda_emu.Module(TEXTURE, barriers=barriers)
     mod.get_texref("tex").set_array(arr)
     pts = np.array([[0.5, 0.5, 0.5], [3.99, 2.2, 1.7], [1.0, 1.0, 0.0], [-3.0, 7.0, 9.0],
                     [2.5, 0.0, 1.2]], dtype=np.float32)
