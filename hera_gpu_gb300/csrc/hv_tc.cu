@@ -607,7 +607,7 @@ __device__ __forceinline__ bool decode_item(const TcParams& p, long long it, int
   return true;
 }
 
-// 18 warps on 4 schedulers: the busiest scheduler holds 5 warps, and its
+// 19 warps on 4 schedulers: the busiest scheduler holds 5 warps, and its
 // 16K-register file caps a thread at 96 registers (launch bounds give that).
 template <bool kCluster, bool kTable>
 __global__ void __launch_bounds__(TC_THREADS, 1)
