@@ -1,5 +1,6 @@
 """The C ABI library: it loads, exports every declared entry point, and the
 Python host layer checks shapes like the reference -- all without a GPU."""
+import ctypes
 import os
 import re
 import subprocess
@@ -102,13 +103,50 @@ def test_median_filter_asserts_before_any_device_work():
 
 
 def test_entry_points_reject_a_null_context(lib):
-    # HV_ERR_ARG (1), without touching CUDA
+    # HV_ERR_ARG (1), checked before any CUDA call
+    ARG = 1
+    d, u, p = ctypes.c_double(), ctypes.c_uint64(), ctypes.c_void_p()
+    assert lib.hv_create(None, 0, 0) == ARG
+    assert lib.hv_vis_gpu(None, 1, 0, None, 4, 1e8, None, 1, None, None, 1, None, 3, None) == ARG
+    assert lib.hv_vis_multifreq(None, 1, 0, None, 4, None, 1, None, 1, None, None, 1, None, 3,
+                                None) == ARG
+    assert lib.hv_vis_multifreq_device(None, 1, 0, None, 4, None, 1, None, 1, None, None, 1, None,
+                                       3, None, None) == ARG
+    assert lib.hv_sync(None) == ARG
+    assert lib.hv_set_profiling(None, 1) == ARG
+    assert lib.hv_profile_read(None, ctypes.byref(d), ctypes.byref(u)) == ARG
+    assert lib.hv_set_wait_limit(None, 0, 0) == ARG
+    assert lib.hv_device_alloc(None, 16, ctypes.byref(p)) == ARG
+    assert lib.hv_device_free(None, None) == ARG
+    assert lib.hv_memcpy_async(None, None, None, 0, 1) == ARG
+    assert lib.hv_stream_query(None) == -ARG
+    assert lib.hv_host_alloc(None, 16, ctypes.byref(p)) == ARG
+    assert lib.hv_host_free(None, None) == ARG
+    assert lib.hv_batch_create(None, None, 1, 0, ctypes.byref(p)) == ARG
+    assert lib.hv_batch_launch(None, None) == ARG
+    assert lib.hv_batch_sync(None) == ARG
+    assert lib.hv_vis_batch(None, None, 1, None) == ARG
     assert lib.hv_omnical(None, 1, None, 0, None, 0, None, 0, None, None, 0, 1e-10, 50, 4, 1,
-                          0.3, None, None, None) == 1
+                          0.3, None, None, None) == ARG
     assert lib.hv_omnical_device(None, 1, None, 0, None, 0, None, 0, None, None, 0, 1e-10, 50,
-                                 4, 1, 0.3, None, None, None, None) == 1
-    assert lib.hv_median_filter(None, None, None, 0, 0, 0, 3, 3) == 1
-    assert lib.hv_median_filter_device(None, None, None, 0, 0, 0, 3, 3, None) == 1
+                                 4, 1, 0.3, None, None, None, None) == ARG
+    assert lib.hv_median_filter(None, None, None, 0, 0, 0, 3, 3) == ARG
+    assert lib.hv_median_filter_device(None, None, None, 0, 0, 0, 3, 3, None) == ARG
+    # nothing to release, nothing counted
+    assert lib.hv_destroy(None) == 0 and lib.hv_batch_destroy(None) == 0
+    assert lib.hv_launch_count(None) == 0 and lib.hv_batch_launches(None) == 0
+    assert lib.hv_last_error(None) == b"no context"
+
+
+def test_noalloc_entry_point_checks_arguments_first(lib):
+    # hv_vis_gpu_noalloc has no context: its errors come back in errbuf
+    buf = ctypes.create_string_buffer(256)
+    assert lib.hv_vis_gpu_noalloc(None, 0, 1e8, None, 1, None, None, 1, None, 3, None, None, buf,
+                                  len(buf)) == 1
+    assert b"bad sizes" in buf.value
+    assert lib.hv_vis_gpu_noalloc(None, 4, 1e8, None, 1, None, None, 1, None, 3, None, None, buf,
+                                  len(buf)) == 1
+    assert b"null array argument" in buf.value
 
 
 @pytest.mark.parametrize("std", ["c99", "c11"])
