@@ -156,3 +156,21 @@ def test_header_is_plain_c(tmp_path, std):
     src.write_text('#include "heravis.h"\nint main(void) { hv_context* c = 0; (void)c; return 0; }\n')
     subprocess.run(["gcc", f"-std={std}", "-Wall", "-Wextra", "-pedantic", "-Werror",
                     "-fsyntax-only", "-I", os.path.join(ROOT, "include"), str(src)], check=True)
+
+
+def test_status_codes_map_to_exceptions(lib):
+    # a Context with no device behind it: only the status -> exception mapping runs
+    ctx = _native.Context.__new__(_native.Context)
+    ctx.lib, ctx.h = lib, None
+    ctx.check(_native.HV_OK)
+    # bad arguments raise AssertionError, as the reference's asserts do
+    with pytest.raises(AssertionError) as e:
+        ctx.check(1)
+    assert isinstance(e.value, _native.HeraVisArgumentError) and e.value.code == 1
+    assert "no context" in str(e.value)
+    with pytest.raises(_native.HeraVisTimeout):
+        ctx.check(4)
+    for code in (2, 3, 5):
+        with pytest.raises(_native.HeraVisError) as e:
+            ctx.check(code)
+        assert type(e.value) is _native.HeraVisError and e.value.code == code
