@@ -174,3 +174,35 @@ def test_status_codes_map_to_exceptions(lib):
         with pytest.raises(_native.HeraVisError) as e:
             ctx.check(code)
         assert type(e.value) is _native.HeraVisError and e.value.code == code
+
+
+def header_enum(name):
+    text = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "heravis.h")).read(),
+                  flags=re.S)
+    return int(re.search(rf"\b{name}\s*=\s*(\d+)", text).group(1))
+
+
+def test_python_constants_match_the_header():
+    for name in ("HV_OK", "HV_ERR_ARG", "HV_ERR_OOM", "HV_ERR_CUDA", "HV_ERR_TIMEOUT",
+                 "HV_ERR_UNSUPPORTED", "HV_BATCH_GRAPH", "HV_BATCH_AUTOTUNE"):
+        assert getattr(_native, name) == header_enum(name), name
+    assert _native.METHODS["auto"] == header_enum("HV_METHOD_AUTO")
+    assert _native.METHODS["plain"] == header_enum("HV_METHOD_PLAIN")
+    assert _native.METHODS["tc"] == _native.METHODS["tc_bf16"] == header_enum("HV_METHOD_TC_BF16")
+
+
+def test_hv_sim_layout_matches_the_header(tmp_path):
+    # the C compiler's layout of hv_sim against the ctypes mirror
+    fields = [f for f, _ in _native.HvSim._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "heravis.h"\nint main(void) {\n'
+                   '  printf("%zu\\n", sizeof(hv_sim));\n'
+                   + "".join(f'  printf("%zu\\n", offsetof(hv_sim, {f}));\n' for f in fields)
+                   + "  return 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    assert got[0] == ctypes.sizeof(_native.HvSim)
+    assert got[1:] == [getattr(_native.HvSim, f).offset for f in fields]
