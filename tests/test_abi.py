@@ -206,3 +206,41 @@ def test_hv_sim_layout_matches_the_header(tmp_path):
                                           check=True).stdout.split()]
     assert got[0] == ctypes.sizeof(_native.HvSim)
     assert got[1:] == [getattr(_native.HvSim, f).offset for f in fields]
+
+
+def _c_kind(decl):
+    decl = " ".join(decl.split())
+    if "*" in decl:
+        return "ptr"
+    for word, kind in (("double", "f64"), ("uint64_t", "u64"), ("size_t", "u64"),
+                       ("unsigned", "u32"), ("int", "i32")):
+        if re.search(rf"\b{word}\b", decl):
+            return kind
+    raise ValueError(decl)
+
+
+def _ctypes_kind(t):
+    if t in (ctypes.c_void_p, ctypes.c_char_p) or (isinstance(t, type) and
+                                                    issubclass(t, ctypes._Pointer)):
+        return "ptr"
+    if t is ctypes.c_double:
+        return "f64"
+    if t in (ctypes.c_size_t, ctypes.c_uint64):
+        return "u64"
+    if t is ctypes.c_uint:
+        return "u32"
+    if t is ctypes.c_int:
+        return "i32"
+    raise ValueError(t)
+
+
+def test_ctypes_signatures_match_the_header_prototypes():
+    text = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "heravis.h")).read(),
+                  flags=re.S)
+    protos = re.findall(r"([A-Za-z_][\w\s\*]*?)\b(hv_\w+)\s*\(([^)]*)\)\s*;", text)
+    assert {name for _, name, _ in protos} == set(_native.SIGNATURES)
+    for ret, name, params in protos:
+        res, args = _native.SIGNATURES[name]
+        params = [] if params.strip() in ("", "void") else params.split(",")
+        assert [_c_kind(p) for p in params] == [_ctypes_kind(a) for a in args], name
+        assert _c_kind(ret) == _ctypes_kind(res), name
