@@ -244,3 +244,14 @@ def test_ctypes_signatures_match_the_header_prototypes():
         params = [] if params.strip() in ("", "void") else params.split(",")
         assert [_c_kind(p) for p in params] == [_ctypes_kind(a) for a in args], name
         assert _c_kind(ret) == _ctypes_kind(res), name
+
+
+def test_integration_guide_binding_matches_the_header():
+    # the ctypes binding INTEGRATION.md shows a maintainer of the reference
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    code = re.search(r"```python\nimport ctypes, numpy as np\n(.*?)```", doc, re.S).group(1)
+    for name in ("hv_create", "hv_vis_gpu"):
+        listed = re.search(rf"_lib\.{name}\.argtypes = (\[.*?\])", code, re.S).group(1)
+        args = eval(listed, {"ctypes": ctypes})
+        assert [_ctypes_kind(a) for a in args] == \
+            [_ctypes_kind(a) for a in _native.SIGNATURES[name][1]], name
