@@ -255,3 +255,36 @@ def test_integration_guide_binding_matches_the_header():
         args = eval(listed, {"ctypes": ctypes})
         assert [_ctypes_kind(a) for a in args] == \
             [_ctypes_kind(a) for a in _native.SIGNATURES[name][1]], name
+
+
+@pytest.mark.parametrize("kwargs,want", [
+    ({}, 1),
+    ({"precision": 2}, 2),
+    ({"real_dtype": np.float64}, 2),
+    ({"real_dtype": np.float32}, 1),
+    ({"complex_dtype": np.complex128}, 2),
+    ({"real_dtype": np.float64, "complex_dtype": np.complex128}, 2),
+    ({"precision": 1, "real_dtype": np.float32, "complex_dtype": np.complex64}, 1),
+])
+def test_precision_spellings(kwargs, want):
+    # the reference's precision (vis.py:147-157) and vis_cpu's dtype spelling
+    from hera_gpu_gb300.vis import _resolve_precision
+    args = {"precision": None, "real_dtype": None, "complex_dtype": None}
+    args.update(kwargs)
+    p, rt, ct = _resolve_precision(args["precision"], args["real_dtype"], args["complex_dtype"])
+    assert p == want
+    assert (rt, ct) == ((np.float32, np.complex64) if want == 1 else (np.float64, np.complex128))
+
+
+@pytest.mark.parametrize("kwargs", [
+    {"precision": 3},
+    {"precision": 1, "real_dtype": np.float64},
+    {"precision": 2, "complex_dtype": np.complex64},
+    {"real_dtype": np.float64, "complex_dtype": np.complex64},
+])
+def test_conflicting_precision_spellings_raise(kwargs):
+    from hera_gpu_gb300.vis import _resolve_precision
+    args = {"precision": None, "real_dtype": None, "complex_dtype": None}
+    args.update(kwargs)
+    with pytest.raises(AssertionError):
+        _resolve_precision(args["precision"], args["real_dtype"], args["complex_dtype"])
