@@ -47,17 +47,23 @@ class ResidentSet:
         self.nant = antpos.shape[0]
         self.P = bm.shape[-1]
         self.freqs = np.asarray(freqs, dtype=np.float64)
-        self.d_antpos = ctx.device_alloc(antpos.nbytes)
-        self.d_bm = ctx.device_alloc(bm.nbytes)
-        ctx.h2d(self.d_antpos, antpos)
-        ctx.h2d(self.d_bm, bm)
-        ctx.sync()
         self.nbytes = antpos.nbytes + bm.nbytes
+        self.d_antpos = self.d_bm = 0
+        try:
+            self.d_antpos = ctx.device_alloc(antpos.nbytes)
+            self.d_bm = ctx.device_alloc(bm.nbytes)
+            ctx.h2d(self.d_antpos, antpos)
+            ctx.h2d(self.d_bm, bm)
+            ctx.sync()
+        except Exception:
+            self.close()    # a failed set holds no device memory
+            raise
 
     def close(self):
-        if self.d_bm:
-            self.ctx.device_free(self.d_antpos)
-            self.ctx.device_free(self.d_bm)
+        if self.d_antpos or self.d_bm:
+            for ptr in (self.d_antpos, self.d_bm):
+                if ptr:
+                    self.ctx.device_free(ptr)
             self.ctx.sync()
             self.d_bm = self.d_antpos = 0
 

@@ -10,6 +10,7 @@ fails only its own requests while the loop keeps serving.
 import types
 
 import numpy as np
+import pytest
 
 from hera_gpu_gb300 import _native, serve
 
@@ -150,3 +151,23 @@ def test_results_handed_to_consumer_without_copy():
     assert all(r.ok and r.delivered and r.result is None for r in done)
     assert all(shape == (r.nfreq, r.ntimes, 20, 20) and mx == 1.0
                for r in done for shape, mx in [seen[r.rid]])
+
+
+def test_a_resident_set_that_fails_to_build_holds_no_device_memory():
+    class FailingSecondAlloc(FakeContext):
+        def device_alloc(self, nbytes):
+            if self.live:
+                raise _native.HeraVisError(_native.HV_ERR_OOM, "injected allocation failure")
+            return super().device_alloc(nbytes)
+
+    ctx = FailingSecondAlloc()
+    with pytest.raises(_native.HeraVisError):
+        serve.ResidentSet(ctx, np.zeros((4, 3)), [1e8], np.zeros((1, 4, 5, 5)))
+    assert ctx.live == {}
+    # a set that builds frees both buffers on close, once
+    ctx = FakeContext()
+    rs = serve.ResidentSet(ctx, np.zeros((4, 3)), [1e8], np.zeros((1, 4, 5, 5)))
+    assert len(ctx.live) == 2
+    rs.close()
+    rs.close()
+    assert ctx.live == {}
