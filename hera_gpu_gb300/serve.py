@@ -120,7 +120,9 @@ BATCH_CHUNK = 65536
 
 def request_bytes(req: Request, nant: int, P: int) -> int:
     """Device memory one request holds while in flight (inputs, output and its
-    share of the batch workspace), for admission against the HBM budget."""
+    share of the batch workspace), for admission against the HBM budget.  The
+    loop's batches are not autotuned, so a slice has ceil(nsrc / BATCH_CHUNK)
+    split-K chunks (an autotuned divisor would multiply them)."""
     Np = -(-nant // 128) * 128
     T, F, S = req.ntimes, req.nfreq, max(req.nsrc, 1)
     nchunk = -(-S // BATCH_CHUNK)  # split-K chunks per slice of the batched kernel

@@ -171,3 +171,11 @@ def test_a_resident_set_that_fails_to_build_holds_no_device_memory():
     rs.close()
     rs.close()
     assert ctx.live == {}
+
+
+def test_batch_chunk_matches_the_library():
+    # admission counts split-K partials with the library's chunk size
+    import os
+    import re
+    src = open(os.path.join(os.path.dirname(serve.__file__), "csrc", "hv_batch.cu")).read()
+    assert int(re.search(r"constexpr int kBatchChunk = (\d+);", src).group(1)) == serve.BATCH_CHUNK
