@@ -7,6 +7,8 @@ a request larger than the budget is rejected, a cancelled request is never
 launched, and a batch that fails (a launch error or a device-side timeout)
 fails only its own requests while the loop keeps serving.
 """
+import os
+import re
 import types
 
 import numpy as np
@@ -175,7 +177,5 @@ def test_a_resident_set_that_fails_to_build_holds_no_device_memory():
 
 def test_batch_chunk_matches_the_library():
     # admission counts split-K partials with the library's chunk size
-    import os
-    import re
     src = open(os.path.join(os.path.dirname(serve.__file__), "csrc", "hv_batch.cu")).read()
     assert int(re.search(r"constexpr int kBatchChunk = (\d+);", src).group(1)) == serve.BATCH_CHUNK
