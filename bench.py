@@ -18,7 +18,16 @@ Arms
                      hera_gpu/tests/test_vis_gpu.py:278-357) on the host
                      cores, on a bounded sample of the same workload.
 
-Several GPUs run independent replicas (the path has no exchange step).
+Also timed: the plain FP32 form on the same step, the array-scale and
+small configurations (350 x 100k x 60 LSTs in FP32, tensor-core and FP64;
+16 x 1000 x 10 LSTs), and each output's error against the FP64 oracle on
+whole (time, channel) slices at the corners of the configuration (first and
+last LST x lowest and highest channel).
+
+Several GPUs run independent replicas (the path has no exchange step):
+``--gpus N`` without a torchrun environment launches N ranks itself through
+torch.distributed.run, one replica per GPU, and the job's time is the
+slowest rank's.
 """
 from __future__ import annotations
 
@@ -77,6 +86,13 @@ def parse_args():
                     help="run only the batched-form leg and print its summary")
     ap.add_argument("--serve-only", action="store_true",
                     help="run only the serving leg and print its summary (profiling runs)")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the array-scale and small-configuration legs")
+    ap.add_argument("--no-corners", action="store_true",
+                    help="skip the per-(time, channel) error check at the configuration's corners")
+    ap.add_argument("--dry-run", action="store_true",
+                    help="launcher check without a GPU: every rank times an empty step over a "
+                         "gloo process group and rank 0 prints the line")
     return ap.parse_args()
 
 
@@ -260,37 +276,93 @@ def job_rate(units_per_rank, world, seconds):
     return world * units_per_rank / seconds
 
 
+def step_config(args, world):
+    """The workload of one step: the same dict in both arms."""
+    return {"workload": f"{args.nant} ant x {args.nsrc} src x {args.nfreq} ch (100-200 MHz), "
+                        f"{T_PER_STEP} of {NTIMES} LSTs per step, beams {BEAM_PX}x{BEAM_PX}",
+            "nant": args.nant, "nsrc": args.nsrc, "nfreq": args.nfreq,
+            "ntimes_per_step": T_PER_STEP, "l2": "inputs larger than L2",
+            "parallelism": f"replicas x{world}"}
+
+
 def run_reference(args):
+    """The reference's CPU algorithm (the oracle port of vis_cpu) on the host
+    cores.  Each step is a bounded sample of the workload: every host process
+    takes a block of CPU_SAMPLE_SRC sources of one (time, channel) slice, in
+    float32 (the reference's default precision=1, hera_gpu/vis.py:146); the
+    rate is extrapolated linearly to the slice's full source count.  One
+    float64 sample (precision=2) is reported beside it."""
     world, rank, _ = dist_setup()
     if rank != 0:
         return 0
     import numpy as np
     pool, cores = cpu_pool()
     w = make_workload(args.nant, args.nsrc, args.nfreq)
-    rates = []
+    rates, walls = [], []
     for i in range(args.warmup + args.steps):
         t = (i * T_PER_STEP) % NTIMES
-        _, wall, nsamp = cpu_sample(pool, cores, w, t, i % args.nfreq)
+        t0 = time.perf_counter()
+        _, span, nsamp = cpu_sample(pool, cores, w, t, i % args.nfreq, "float32")
         if i >= args.warmup:
-            rates.append(cpu_rate(wall, nsamp, args.nant, args.nsrc))
+            walls.append(time.perf_counter() - t0)
+            rates.append(cpu_rate(span, nsamp, args.nant, args.nsrc))
+    _, span64, nsamp64 = cpu_sample(pool, cores, w, 0, 0, "float64")
     pool.close()
     value = float(np.mean(rates))
     sample = (f"{cores} host processes x {CPU_SAMPLE_SRC} sources of one (time, channel) slice "
-              f"per step, extrapolated linearly to {args.nsrc} sources")
+              f"per step in float32 (the reference's default precision 1), extrapolated "
+              f"linearly to {args.nsrc} sources; ms_per_step is the sample's wall time")
     line = {
         "impl": "reference", "metric": "visibilities/s", "value": value, "unit": "vis/s",
         "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * T_PER_STEP * args.nfreq * args.nant ** 2 / value,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded)",
-        "config": {"workload": f"{args.nant} ant x {args.nsrc} src x {args.nfreq} ch, "
-                               f"{T_PER_STEP} LSTs per step", "nant": args.nant,
-                   "nsrc": args.nsrc, "nfreq": args.nfreq},
+        "ms_per_step": 1e3 * float(np.mean(walls)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)", "method": "cpu",
+        "config": step_config(args, world),
         "cpu_baseline": {"value": value, "unit": "vis/s", "cores": cores, "kind": "port",
-                         "sample": sample},
+                         "sample": sample,
+                         "value_fp64": cpu_rate(span64, nsamp64, args.nant, args.nsrc)},
         "e2e": {"value": value, "unit": "vis/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+    return 0
+
+
+def launch_replicas(args):
+    """``--gpus N`` outside a torchrun environment: run this script as N
+    ranks through torch.distributed.run (one replica per GPU, rendezvous on
+    127.0.0.1) and return its exit status; None when this process is already
+    a rank (or N is 1)."""
+    if args.gpus <= 1 or "WORLD_SIZE" in os.environ:
+        return None
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+           f"--nproc-per-node={args.gpus}", "--master-addr", "127.0.0.1",
+           "--master-port", str(port), os.path.abspath(__file__), *sys.argv[1:]]
+    return subprocess.call(cmd)
+
+
+def run_dry(args):
+    """The replica launcher and the max-over-ranks timing without a GPU:
+    each rank times an empty step; rank 0 prints a line with n_gpus = the
+    number of ranks."""
+    import torch
+    import torch.distributed as dist
+    world, rank, _ = dist_setup()
+    if world > 1:
+        dist.init_process_group("gloo")
+    t0 = time.perf_counter()
+    time.sleep(0.01 * (rank + 1))
+    ms = max_over_ranks(1e3 * (time.perf_counter() - t0))
+    if rank == 0:
+        print(json.dumps({"metric": "visibilities/s", "dry_run": True, "n_gpus": world,
+                          "ms_per_step": ms, "config": step_config(args, world)}), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    del torch
     return 0
 
 
@@ -301,17 +373,13 @@ def load_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-def load_traffic():
-    """DRAM bytes per (slice x source above the horizon) of the fused kernel,
-    from the committed ncu summary (None if absent)."""
-    path = os.path.join(ROOT, "profiles", "tc_vis_kernel.md")
-    try:
-        for ln in open(path):
-            if ln.startswith("dram_bytes_per_slice_source:"):
-                return float(ln.split(":", 1)[1].split()[0])
-    except OSError:
-        pass
-    return None
+# DRAM bytes per unit of work (slice x source above the horizon) of one
+# fused-kernel launch, measured once with ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum of the cluster launch on 350 antennas x 1,048,576
+# sources x 16 channels x 4 LSTs, 2.285 GB over 31,354,782 units): the
+# bench cannot read DRAM counters itself, so the figure is carried here and
+# scaled by the units each timed launch processed.
+TC_DRAM_BYTES_PER_UNIT = {"tc": 72.885}
 
 
 def run_ours(args):
@@ -338,8 +406,8 @@ def run_ours(args):
     # a stream of our own: the library launches on it and the events time it
     stream = torch.cuda.Stream(dev)
 
-    def step(i, method):
-        t0 = (i * T_PER_STEP) % NTIMES
+    def step(i, method, t0=None):
+        t0 = (i * T_PER_STEP) % NTIMES if t0 is None else t0
         ctx.vis_multifreq_device(1, method, d["antpos"].data_ptr(), N, w["freqs"],
                                  d["eq2tops"][t0:t0 + T_PER_STEP].data_ptr(), T_PER_STEP,
                                  d["crd_eq"].data_ptr(), d["I_sky"].data_ptr(), S,
@@ -371,10 +439,6 @@ def run_ours(args):
         barrier()
     ms = ev0.elapsed_time(ev1)
     ctx.sync()
-    # one (time, channel) slice of the timed output, for its error against
-    # the FP64 oracle below: channel 0 at the first LST of the last step
-    t_check = times[-1]
-    V_check = {args.method: d_out[0, 0].cpu().numpy()}
     kern_ms, kern_launches = ctx.profile_read()
     ctx.set_profiling(False)
     launches = ctx.launches - l0
@@ -395,7 +459,7 @@ def run_ours(args):
                      for su in s_up) * F
         hw_flops = stages * 12 * 2 * 128 * 16 * sum(tc_groups(N))
         peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
-        traffic_unit = load_traffic()
+        traffic_unit = TC_DRAM_BYTES_PER_UNIT.get(args.method)
         units = sum(s_up) * F
         roof = {"bound": "tensor", "achieved": herk_flops / (kern_ms / 1e3) / 1e12,
                 "peak": peak, "unit": "TFLOP/s",
@@ -422,11 +486,7 @@ def run_ours(args):
         "dtype": "bf16" if args.method == "tc" else "fp32",
         "data": "synthetic (seeded); inputs larger than L2 (beam cubes "
                 f"{w['bm_cubes'].nbytes / 1e6:.0f} MB)",
-        "config": {"workload": f"{N} ant x {S} src x {F} ch (100-200 MHz), {T_PER_STEP} of "
-                               f"{NTIMES} LSTs per step, beams {BEAM_PX}x{BEAM_PX}",
-                   "nant": N, "nsrc": S, "nfreq": F, "ntimes_per_step": T_PER_STEP,
-                   "method": args.method, "l2": "inputs larger than L2",
-                   "parallelism": f"replicas x{world}"},
+        "method": args.method, "config": step_config(args, world),
         "roofline": roof, "clocks": clk, "gpu_launches": launches,
         # the reference returns the full N x N matrix (the metric above); the
         # distinct baselines a b >= a of it are N (N + 1) / 2 of those
@@ -468,11 +528,10 @@ def run_ours(args):
         ctx.profile_read()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        t_plain = step(1, "plain")
+        step(1, "plain")
         e1.record(stream)
         torch.cuda.synchronize(dev)
         pms = e0.elapsed_time(e1)
-        V_check["plain"] = d_out[0, 0].cpu().numpy()
         pk_ms, _ = ctx.profile_read()
         ctx.set_profiling(False)
         pflops = sum(4.0 * N * (N + 1) * sources_up(w, T_PER_STEP + k) * F
@@ -482,31 +541,54 @@ def run_ours(args):
                               "herk_tflops": pflops / (pk_ms / 1e3) / 1e12,
                               "tc_speedup": value / world / (vis_per_step / (pms / 1e3))}
 
-    # ---- CPU baseline: the FP64 oracle of whole slices of the workload,
-    # which also gives the error of the timed output (same inputs, all S
-    # sources, the split-K chunking of the benchmark) ----------------------
+    # ---- error against the FP64 oracle at the corners of the configuration
+    # (first and last LST x lowest and highest channel), whole slices with
+    # all S sources, each form's output from a call of the timed shape (4
+    # LSTs x all channels, the benchmark's own split-K chunking) -------------
     if rank == 0 and pool is not None:
-        V_ref, wall, nsamp = cpu_sample(pool, cores, w, t_check, 0, nsamp=S)
-        _, wall32, nsamp32 = cpu_sample(pool, cores, w, 0, 0, "float32")
-        line["cpu_baseline"] = {
-            "value": cpu_rate(wall, nsamp, N, S), "unit": "vis/s", "cores": cores,
-            "kind": "port",
-            "value_fp32": cpu_rate(wall32, nsamp32, N, S),
-            "sample": f"value: the float64 oracle of one whole slice (LST {t_check}, "
-                      f"{w['freqs'][0] / 1e6:.0f} MHz, {S} sources) on {cores} processes; "
-                      f"value_fp32: float32 on {nsamp32} sources of a slice, extrapolated "
-                      f"linearly to {S}"}
-        rel = lambda v, r: float(np.linalg.norm(v - r) / np.linalg.norm(r))
+        methods = [args.method] + (["plain"] if not args.no_plain and args.method != "plain"
+                                   else [])
+        corners = [(0, 0), (0, F - 1), (NTIMES - 1, 0), (NTIMES - 1, F - 1)]
+        if args.no_corners:
+            corners = corners[:1]
+        got = {m: {} for m in methods}
+        for m in methods:
+            for t0 in sorted({min(t, NTIMES - T_PER_STEP) for t, _ in corners}):
+                step(0, m, t0)
+                ctx.sync()
+                for t, f in corners:
+                    if t0 <= t < t0 + T_PER_STEP:
+                        got[m][(t, f)] = d_out[f, t - t0].cpu().numpy()
         herm = lambda V: np.triu(V) + np.triu(V, 1).conj().T   # the library's orientation
-        errs = {args.method: rel(V_check[args.method], herm(V_ref))}
-        if "plain" in V_check:
-            V_ref_p = V_ref if t_plain == t_check else \
-                cpu_sample(pool, cores, w, t_plain, 0, nsamp=S)[0]
-            errs["plain"] = rel(V_check["plain"], herm(V_ref_p))
+        rel = lambda v, r: float(np.linalg.norm(v - r) / np.linalg.norm(r))
+        errs = {m: [] for m in methods}
+        spans = []
+        for t, f in corners:
+            V_ref, span, _ = cpu_sample(pool, cores, w, t, f, nsamp=S)
+            spans.append(span)
+            for m in methods:
+                errs[m].append({"lst_index": t, "mhz": round(float(w["freqs"][f]) / 1e6, 3),
+                                "err": rel(got[m][(t, f)], herm(V_ref))})
         line["rel_err_vs_fp64"] = {
-            **errs, "sample": f"one whole slice of the timed output ({N} ant x {S} src, "
-                              f"LST {t_check}, {w['freqs'][0] / 1e6:.0f} MHz) against the FP64 "
-                              f"oracle of the same inputs"}
+            **{m: max(e["err"] for e in errs[m]) for m in methods},
+            "per_slice": errs,
+            "bound": {"tc": 1e-4, "plain": 1e-5},
+            "sample": f"whole slices ({N} ant x {S} src) at (LST index, channel) "
+                      f"{[(t, f) for t, f in corners]} of outputs of the timed call shape, against "
+                      f"the FP64 oracle of the same inputs; the headline key is the largest"}
+        _, span32, nsamp32 = cpu_sample(pool, cores, w, 0, 0, "float32")
+        line["cpu_baseline"] = {
+            "value": cpu_rate(span32, nsamp32, N, S), "unit": "vis/s", "cores": cores,
+            "kind": "port",
+            "value_fp64": cpu_rate(min(spans), S, N, S),
+            "sample": f"value: the oracle port in float32 (the reference's default precision 1) "
+                      f"on {nsamp32} sources of one slice on {cores} processes, extrapolated "
+                      f"linearly to {S}; value_fp64: the float64 oracle of one whole slice "
+                      f"({S} sources) on {cores} processes"}
+
+    # ---- the small and array-scale configurations ---------------------------
+    if rank == 0 and not args.no_configs:
+        line["configs"] = run_configs(args, local, pool, cores)
 
     # ---- batched form: many uneven simulations in one plan ----------------
     if rank == 0 and args.batch_sims > 0:
@@ -531,6 +613,122 @@ def run_ours(args):
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+# The reference's published vis_gpu timings (hera_gpu/tests/speed_test_output.txt:
+# 15, 22; hardware unstated): one call of 350 antennas x 314,159 sources x 10
+# LSTs took 0.934 s in FP32 and 13.04 s in FP64.
+PUBLISHED_SHAPE = dict(nant=350, nsrc=314_159, ntimes=10)
+PUBLISHED_S = {1: 0.934, 2: 13.04}
+
+
+def run_configs(args, device, pool, cores):
+    """The other configurations, each form timed through the device entry
+    point (inputs resident, CUDA events on the call's stream, one step = one
+    call over all of the configuration's LSTs) and once through the drop-in
+    vis_gpu with host arrays (copies included); each output's error against
+    the FP64 oracle on its first and last LST (whole slices); the oracle
+    port on the host cores as the CPU baseline.
+
+      small      16 antennas, 1000 sources, 10 LSTs, 31x31 Gaussian beams,
+                 150 MHz
+      array      350 antennas, 100,000 sources, 60 LSTs, 63x63 Airy beams,
+                 150 MHz, FP32 (plain and tensor-core) and FP64
+      published  the shape of the reference's own timings (350 x 314,159 x
+                 10 LSTs, 63x63 Airy beams, 150 MHz), beside its published
+                 seconds per call (other, unstated hardware)"""
+    import numpy as np
+    import torch
+    from hera_gpu_gb300 import _native, synth, vis_gpu
+    from oracle import vis_oracle
+    dev = torch.device("cuda", device)
+    ctx = _native.Context(device)
+    stream = torch.cuda.Stream(dev)
+    small = synth.config_small(seed=0)
+    arr = synth.config_array(seed=2, nant=350, nsrc=100_000, ntimes=60, nfreq=1, fmin=150e6,
+                             fmax=150e6, P=63)
+    arr["bm_cubes"] = synth.beams_for(arr, dtype=np.float64)
+    pub = synth.config_array(seed=3, nfreq=1, fmin=150e6, fmax=150e6, P=63, **PUBLISHED_SHAPE)
+    pub["bm_cubes"] = synth.beams_for(pub, dtype=np.float64)
+    forms = [("plain", 1), ("tc", 1), ("plain", 2)]
+    plan = {"small": (small, 20, 3), "array": (arr, 3, 1), "published": (pub, 2, 1)}
+    out = {}
+    for name, (c, steps, warm) in plan.items():
+        N, S, T = c["antpos"].shape[0], c["crd_eq"].shape[1], c["eq2tops"].shape[0]
+        freq = float(c["freqs"][0])
+        res = {"nant": N, "nsrc": S, "ntimes": T, "beam_px": c["bm_cubes"].shape[-1],
+               "mhz": freq / 1e6, "forms": {}}
+        refs = {}
+        for method, prec in forms:
+            rt = np.float32 if prec == 1 else np.float64
+            ct = torch.complex64 if prec == 1 else torch.complex128
+            host = {k: np.ascontiguousarray(c[k], dtype=rt)
+                    for k in ("antpos", "eq2tops", "crd_eq", "I_sky")}
+            host["bm"] = np.ascontiguousarray(c["bm_cubes"], dtype=rt)
+            d = {k: torch.from_numpy(v).to(dev) for k, v in host.items()}
+            o = torch.empty((1, T, N, N), dtype=ct, device=dev)
+            n_steps = 1 if prec == 2 and name != "small" else steps
+
+            def call():
+                ctx.vis_multifreq_device(prec, method, d["antpos"].data_ptr(), N, [freq],
+                                         d["eq2tops"].data_ptr(), T, d["crd_eq"].data_ptr(),
+                                         d["I_sky"].data_ptr(), S, d["bm"].data_ptr(),
+                                         host["bm"].shape[-1], o.data_ptr(), stream.cuda_stream)
+            for _ in range(warm):
+                call()
+            ctx.sync()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(n_steps):
+                call()
+            e1.record(stream)
+            ctx.sync()
+            ms = e0.elapsed_time(e1) / n_steps
+            t0 = time.perf_counter()
+            V = vis_gpu(host["antpos"], freq, host["eq2tops"], host["crd_eq"], host["I_sky"],
+                        host["bm"][0], precision=prec, method=method, context=ctx)
+            e2e_s = time.perf_counter() - t0
+            key = f"{method}_fp{32 * prec}"
+            form = {"ms_per_call": ms, "vis_per_s": T * N * N / (ms / 1e3),
+                    "e2e_vis_per_s": T * N * N / e2e_s, "steps": n_steps}
+            if name == "published":
+                form["reference_published_s"] = PUBLISHED_S[prec]
+            # error on the first and last LST against the FP64 oracle of the
+            # inputs as the GPU saw them
+            errs = []
+            for t in (0, T - 1):
+                rk = (prec, t)
+                if rk not in refs:
+                    seen = {k: np.asarray(v, dtype=np.float64) for k, v in host.items()}
+                    if pool is not None and S > 20000:
+                        ws = dict(antpos=seen["antpos"], freqs=np.array([freq]),
+                                  eq2tops=seen["eq2tops"], crd_eq=seen["crd_eq"],
+                                  I_sky=seen["I_sky"], bm_cubes=seen["bm"])
+                        Vr = cpu_sample(pool, cores, ws, t, 0, nsamp=S)[0]
+                        refs[rk] = np.triu(Vr) + np.triu(Vr, 1).conj().T
+                    else:
+                        refs[rk] = vis_oracle(seen["antpos"], freq, seen["eq2tops"][t:t + 1],
+                                              seen["crd_eq"], seen["I_sky"], seen["bm"][0])[0]
+                ref = refs[rk]
+                errs.append(float(np.linalg.norm(V[t] - ref) / np.linalg.norm(ref)))
+            form["rel_err_vs_fp64"] = max(errs)
+            res["forms"][key] = form
+        # the oracle port on the host cores, float32 and float64
+        if pool is not None:
+            cpu = {}
+            for dt in ("float32", "float64"):
+                ws = dict(antpos=c["antpos"], freqs=np.array([freq]), eq2tops=c["eq2tops"],
+                          crd_eq=c["crd_eq"], I_sky=c["I_sky"], bm_cubes=c["bm_cubes"])
+                _, span, nsamp = cpu_sample(pool, cores, ws, 0, 0, dt,
+                                            nsamp=min(S, cores * CPU_SAMPLE_SRC))
+                cpu[dt] = cpu_rate(span, nsamp, N, S)
+            res["cpu_baseline"] = {"vis_per_s_fp32": cpu["float32"], "vis_per_s_fp64": cpu["float64"],
+                                   "cores": cores, "kind": "port",
+                                   "sample": f"one slice on {cores} processes"
+                                             + (", extrapolated linearly in sources"
+                                                if S > cores * CPU_SAMPLE_SRC else "")}
+        out[name] = res
+    return out
 
 
 # the largest images and windows of the reference's median-filter tests
@@ -823,6 +1021,11 @@ def run_serve(args, device, pool):
 
 def main():
     args = parse_args()
+    rc = launch_replicas(args)
+    if rc is not None:
+        return rc
+    if args.dry_run:
+        return run_dry(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.serve_only:

@@ -55,6 +55,10 @@ int report(char* buf, size_t len, int code, const char* fmt, ...) {
 
 size_t up256(size_t x) { return (x + 255) & ~size_t(255); }
 
+// The frequency goes to the device as a kernel argument: no copy from host
+// memory is queued, so nothing of the call reads the caller's stack later.
+__global__ void set_freq_kernel(double* d_freq, double freq) { *d_freq = freq; }
+
 }  // namespace
 
 extern "C" int hv_vis_gpu_noalloc(const void* d_antpos, int nant, double freq,
@@ -64,7 +68,9 @@ extern "C" int hv_vis_gpu_noalloc(const void* d_antpos, int nant, double freq,
                                   size_t errlen) {
   using namespace hv;
   if (errbuf && errlen) errbuf[0] = '\0';
-  if (nant < 1 || ntimes < 0 || nsrc < 0 || beam_px < 1 || beam_px > 4096)
+  // the limits of the allocating entry points (check_shapes in hv_api.cu),
+  // checked before any size is computed so that no product below overflows
+  if (nant < 1 || nant > 65536 || ntimes < 0 || nsrc < 0 || beam_px < 1 || beam_px > 4096)
     return report(errbuf, errlen, HV_ERR_ARG,
                   "bad sizes (nant %d, ntimes %d, nsrc %d, beam_px %d)", nant, ntimes, nsrc,
                   beam_px);
@@ -133,7 +139,8 @@ extern "C" int hv_vis_gpu_noalloc(const void* d_antpos, int nant, double freq,
     if (e_ != cudaSuccess)                                                             \
       return report(errbuf, errlen, HV_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
   } while (0)
-  HV_NA_CK(cudaMemcpyAsync(d_freq, &freq, sizeof(double), cudaMemcpyHostToDevice, st));
+  set_freq_kernel<<<1, 1, 0, st>>>(d_freq, freq);
+  HV_NA_CK(cudaGetLastError());
   HV_NA_CK(launch_beam_transpose<float>(static_cast<const float*>(d_bm_cube), 1, nant, beam_px,
                                         Np, beamT, st));
   HV_NA_CK(launch_ucoef<float>(antpos, nant, Np, e2t, 0, ntimes, d_freq, 1, U, st));

@@ -29,7 +29,21 @@ MAX_MEMORY = 2 ** 29
 MIN_CHUNK = 8
 
 
+def _as_dtype(x, name):
+    """np.dtype(x), or an AssertionError naming the argument: a reference
+    caller passing ``nthreads`` positionally lands an integer here."""
+    try:
+        return np.dtype(x)
+    except TypeError:
+        raise AssertionError(f"{name} must be a dtype (got {x!r}); nthreads, max_memory, "
+                             "precision and verbose are keyword arguments here") from None
+
+
 def _resolve_precision(precision, real_dtype, complex_dtype):
+    if real_dtype is not None:
+        real_dtype = _as_dtype(real_dtype, "real_dtype")
+    if complex_dtype is not None:
+        complex_dtype = _as_dtype(complex_dtype, "complex_dtype")
     if precision is None:
         if real_dtype is not None:
             precision = 2 if np.dtype(real_dtype) == np.float64 else 1

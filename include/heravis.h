@@ -10,7 +10,7 @@
  *
  * The reference exposes that path as a Python function only; these entry
  * points are what a foreign-function binding of it binds (the ctypes binding
- * shipped in hera_gpu_gb300/_native.py, and the stubs in INTEGRATION.md).
+ * shipped in hera_gpu_gb300/_native.py is one).
  *
  * Conventions
  *  - Every call returns an hv_status; hv_last_error() gives the message of the

@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 from hera_gpu_gb300 import _native, vis_gpu
+from noalloc_sizes import SCRATCH_BYTES, largest_nsrc, need_bytes
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -147,6 +148,25 @@ def test_noalloc_entry_point_checks_arguments_first(lib):
     assert lib.hv_vis_gpu_noalloc(None, 4, 1e8, None, 1, None, None, 1, None, 3, None, None, buf,
                                   len(buf)) == 1
     assert b"null array argument" in buf.value
+    # the antenna limit of the allocating entry points, before any size is formed
+    for nant in (65537, 2**31 - 1):
+        assert lib.hv_vis_gpu_noalloc(None, nant, 1e8, None, 1, None, None, 1, None, 3, None, None,
+                                      buf, len(buf)) == 1
+        assert b"bad sizes" in buf.value
+
+
+def test_noalloc_refuses_one_source_past_its_array(lib):
+    # a request one source past the largest that fits is refused by the size
+    # check, which comes before any CUDA call (the pointers are never read)
+    nant, ntimes, P = 150, 2, 31
+    nsrc = largest_nsrc(nant, ntimes, P)
+    assert need_bytes(nant, nsrc + 1, ntimes, P) > SCRATCH_BYTES
+    buf = ctypes.create_string_buffer(512)
+    one = ctypes.c_void_p(1)
+    assert lib.hv_vis_gpu_noalloc(one, nant, 1e8, one, ntimes, one, one, nsrc + 1, one, P, one,
+                                  None, buf, len(buf)) == 1
+    assert b"working memory" in buf.value
+    assert str(need_bytes(nant, nsrc + 1, ntimes, P)).encode() in buf.value
 
 
 @pytest.mark.parametrize("std", ["c99", "c11"])
@@ -288,3 +308,12 @@ def test_conflicting_precision_spellings_raise(kwargs):
     args.update(kwargs)
     with pytest.raises(AssertionError):
         _resolve_precision(args["precision"], args["real_dtype"], args["complex_dtype"])
+
+
+def test_positional_nthreads_of_a_reference_caller_is_an_assertion():
+    # the reference takes nthreads at position 7 (vis.py:144-146); here that
+    # position is real_dtype, so an integer there is refused as the
+    # reference refuses bad arguments, before any device work
+    with pytest.raises(AssertionError, match="keyword"):
+        vis_gpu(np.zeros((2, 3)), 1e8, np.zeros((1, 3, 3)), np.zeros((3, 4)), np.zeros(4),
+                np.zeros((2, 3, 3)), 1024)

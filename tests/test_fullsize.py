@@ -12,13 +12,17 @@
       A_a(l, m)^2 I carry no phase, so the oracle computes them at full size
       (beam interpolation only);
     - the product is linear in the sources: the visibilities of all sources
-      equal the sum of those of two halves.
+      equal the sum of those of two halves;
+  and through whole slices against the FP64 oracle, cross-correlations
+  included: the lowest channel (100 MHz) at the first LST and the highest
+  (200 MHz, twice the phase range) at the second, every one of the 1,048,576
+  sources (the oracle sums them in blocks to bound its memory).
 """
 import numpy as np
 import pytest
 
 from hera_gpu_gb300 import synth, vis_gpu, vis_gpu_multifreq
-from oracle import bilinear_beam, rel_frobenius, vis_oracle
+from oracle import bilinear_beam, rel_frobenius, vis_oracle, vis_oracle_partial
 
 pytestmark = pytest.mark.gpu
 
@@ -58,6 +62,25 @@ def test_fullsize_autocorrelations(full, t, f):
     got = np.diagonal(V[f, t]).real.astype(np.float64)
     err = np.abs(got - ref) / ref
     assert err.max() <= 1e-4, err.max()
+
+
+def oracle_slice(args, t, f, block=131072):
+    """FP64 oracle of slice (t, f) of the full-size call over all sources, in
+    the library's orientation (upper triangle computed, lower its conjugate)."""
+    antpos, freqs, e2t, crd, I, bm = args
+    a64 = lambda x: np.asarray(x, dtype=np.float64)
+    V = 0
+    for s0 in range(0, crd.shape[1], block):
+        V = V + vis_oracle_partial(a64(antpos), float(freqs[f]), a64(e2t[t]), a64(crd[:, s0:s0 + block]),
+                                   a64(I[s0:s0 + block]), a64(bm[f]), 0, min(block, crd.shape[1] - s0))
+    return np.triu(V) + np.triu(V, 1).conj().T
+
+
+@pytest.mark.parametrize("t,f", [(0, 0), (1, 63)])
+def test_fullsize_slice_against_oracle(full, t, f):
+    args, V = full
+    err = rel_frobenius(V[f, t], oracle_slice(args, t, f))
+    assert err <= 1e-4, err
 
 
 def test_fullsize_linear_in_the_sources(full):

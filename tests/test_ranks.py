@@ -62,3 +62,29 @@ def test_reference_arm_under_torchrun_reports_once():
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+    # the same workload description as the GPU arm's (bench.step_config),
+    # and a step time that is the measured sample's, not an extrapolation
+    import argparse
+    sys.path.insert(0, ROOT)
+    import bench
+    assert line["config"] == bench.step_config(argparse.Namespace(nant=16, nsrc=2048, nfreq=2), 2)
+    assert line["dtype"] == "f32" and line["cpu_baseline"]["value_fp64"] > 0
+    assert line["ms_per_step"] < 60e3
+
+
+def test_gpus_flag_launches_the_replicas_itself():
+    # `bench.py --gpus 2` outside torchrun starts two ranks through
+    # torch.distributed.run; the dry run needs no GPU (gloo), and the line
+    # reports both ranks and the slowest rank's time
+    r = subprocess.run([sys.executable, "bench.py", "--gpus", "2", "--dry-run"], cwd=ROOT,
+                       capture_output=True, text=True, timeout=600,
+                       env={k: v for k, v in os.environ.items()
+                            if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")})
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert line["n_gpus"] == 2 and line["dry_run"]
+    assert line["ms_per_step"] >= 20.0          # rank 1 sleeps 20 ms
+    assert line["config"]["parallelism"] == "replicas x2"
+

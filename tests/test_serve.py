@@ -3,7 +3,8 @@
 Requests that arrive close together are served in shared batches on two
 slots; every result must equal the result of the same request served alone
 (each simulation of a batch keeps its own work items and reduction order),
-and agree with the FP64 oracle within the tensor-core tolerance.
+and agree with the FP64 oracle within the tensor-core tolerance on every
+channel and time it asked for.
 """
 import numpy as np
 import pytest
@@ -60,11 +61,13 @@ def test_server_matches_oracle():
         full = serve.synth.hex_array(350, 14.6, 0.01, rng)
         pick = np.sort(rng.choice(350, size=sp["nant"], replace=False))
         dish = 14.0 * (1.0 + 0.02 * rng.uniform(-1.0, 1.0, sp["nant"]))
-        f0 = sets[r.set_id].freqs[0]
-        bm = serve.synth.airy_beams(sp["nant"], sp["P"], f0, dish).astype(np.float32)
-        ref = vis_oracle(full[pick].astype(np.float32).astype(np.float64), f0,
-                         r.eq2tops.astype(np.float64), r.crd_eq.astype(np.float64),
-                         r.I_sky.astype(np.float64), bm.astype(np.float64))
-        assert rel_frobenius(r.result[0], ref).max() <= 1e-4
+        assert r.result.shape == (r.nfreq, r.ntimes, sp["nant"], sp["nant"])
+        for f in range(r.nfreq):  # every channel of the request, every time
+            fq = sets[r.set_id].freqs[f]
+            bm = serve.synth.airy_beams(sp["nant"], sp["P"], fq, dish).astype(np.float32)
+            ref = vis_oracle(full[pick].astype(np.float32).astype(np.float64), fq,
+                             r.eq2tops.astype(np.float64), r.crd_eq.astype(np.float64),
+                             r.I_sky.astype(np.float64), bm.astype(np.float64))
+            assert rel_frobenius(r.result[f], ref).max() <= 1e-4, (r.rid, f)
     for s in sets:
         s.close()

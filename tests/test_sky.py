@@ -85,3 +85,42 @@ def test_lst_grid_and_stack():
     e = sky.eq2tops(g, 0.1)
     assert e.shape == (5, 3, 3)
     np.testing.assert_array_equal(e[2], sky.eq2top(g[2], 0.1))
+
+
+# HERA simulators build eq2tops with aipy's coordinate convention,
+# eq2top_m(ha, dec) evaluated at ha = -LST and dec = latitude: the passive
+# rotation R_x(pi/2 - dec) R_z(pi/2 - ha) (R_z turns the x axis to the east
+# of the meridian, R_x tilts the pole to the observer's latitude).  Golden
+# values of that convention, computed from the rotation product and rounded
+# to 15 digits: (LST rad, latitude deg) -> matrix.
+AIPY_CONVENTION_GOLDEN = {
+    (0.0, -30.72): [[0.0, 1.0, 0.0], [0.51084303186586, 0.0, 0.859674006117491],
+                    [0.859674006117491, 0.0, -0.51084303186586]],
+    (1.0, -30.72): [[-0.841470984807896, 0.54030230586814, 0.0],
+                    [0.276009668053796, 0.429859589106417, 0.859674006117491],
+                    [0.464483847800182, 0.723390732541435, -0.51084303186586]],
+    (4.2, 52.0): [[0.871575772413588, -0.4902608213407, 0.0],
+                  [0.386330799288535, 0.686811081244992, 0.615661475325658],
+                  [-0.301834700560984, -0.53659562590225, 0.788010753606722]],
+    (2.5, 0.0): [[-0.598472144103956, -0.801143615546934, 0.0], [0.0, 0.0, 1.0],
+                 [-0.801143615546934, 0.598472144103956, 0.0]],
+}
+
+
+def _rot_x(b):
+    c, s = np.cos(b), np.sin(b)
+    return np.array([[1.0, 0.0, 0.0], [0.0, c, s], [0.0, -s, c]])
+
+
+def _rot_z(a):
+    c, s = np.cos(a), np.sin(a)
+    return np.array([[c, s, 0.0], [-s, c, 0.0], [0.0, 0.0, 1.0]])
+
+
+@pytest.mark.parametrize("key", sorted(AIPY_CONVENTION_GOLDEN))
+def test_eq2top_is_the_aipy_convention_of_hera_callers(key):
+    lst, lat_deg = key
+    got = sky.eq2top(lst, np.radians(lat_deg))
+    np.testing.assert_allclose(got, AIPY_CONVENTION_GOLDEN[key], atol=2e-15)
+    ha, dec = -lst, np.radians(lat_deg)
+    np.testing.assert_allclose(got, _rot_x(np.pi / 2 - dec) @ _rot_z(np.pi / 2 - ha), atol=1e-15)
