@@ -32,6 +32,7 @@ slowest rank's.
 from __future__ import annotations
 
 import argparse
+import contextlib
 import json
 import math
 import os
@@ -61,7 +62,9 @@ def parse_args():
     ap.add_argument("--nsrc", type=int, default=NSRC)
     ap.add_argument("--nfreq", type=int, default=NFREQ)
     ap.add_argument("--nant", type=int, default=NANT)
-    ap.add_argument("--method", default="tc", choices=["tc", "plain"])
+    ap.add_argument("--method", default="tc", choices=["tc", "tc_fp16", "plain"])
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip timing the other fused form on the same steps")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
@@ -420,74 +423,94 @@ def run_ours(args):
         if world > 1:
             torch.distributed.barrier()
 
-    # ---- device-resident throughput of the chosen form -------------------
-    for i in range(args.warmup):
-        step(i, args.method)
-    ctx.sync()
-    barrier()
-    ctx.set_profiling(True)
-    ctx.profile_read()
-    l0 = ctx.launches
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    times = []
-    with ClockSampler(local) as clocks:
-        barrier()
-        ev0.record(stream)
-        for i in range(args.warmup, args.warmup + args.steps):
-            times.append(step(i, args.method))
-        ev1.record(stream)
-        barrier()
-    ms = ev0.elapsed_time(ev1)
-    ctx.sync()
-    kern_ms, kern_launches = ctx.profile_read()
-    ctx.set_profiling(False)
-    launches = ctx.launches - l0
-    ms = max_over_ranks(ms, dev)
+    # ---- device-resident throughput of a form --------------------------------
     vis_per_step = T_PER_STEP * F * N * N
-    value = job_rate(args.steps * vis_per_step, world, ms / 1e3)
-    clk = clocks.summary()
-
-    # ---- roofline of the contraction kernel -------------------------------
     peaks, peak_src = load_peaks()
-    s_up = [sources_up(w, t0 + k) for t0 in times for k in range(T_PER_STEP)]
-    herk_flops = sum(4.0 * N * (N + 1) * su * F for su in s_up)
-    if args.method == "tc":
-        ng = tc_num_groups(N)
-        chunk = tc_chunk(S, T_PER_STEP * F, ng, num_sms)
-        # 16-source stages of 12 MMAs (3 split products x 4 real products)
-        stages = sum(sum(math.ceil(min(chunk, su - k0) / 16) for k0 in range(0, su, chunk))
-                     for su in s_up) * F
-        hw_flops = stages * 12 * 2 * 128 * 16 * sum(tc_groups(N))
-        peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
-        traffic_unit = TC_DRAM_BYTES_PER_UNIT.get(args.method)
-        units = sum(s_up) * F
-        roof = {"bound": "tensor", "achieved": herk_flops / (kern_ms / 1e3) / 1e12,
-                "peak": peak, "unit": "TFLOP/s",
-                "frac": herk_flops / (kern_ms / 1e3) / 1e12 / peak,
-                "traffic": (traffic_unit * units / kern_launches) if traffic_unit else None,
-                "kernel": "tc_vis_kernel", "launches": kern_launches,
-                "kernel_ms": kern_ms,
-                "hw_tflops": hw_flops / (kern_ms / 1e3) / 1e12,
-                "hw_frac": hw_flops / (kern_ms / 1e3) / 1e12 / peak,
-                "peak_kind": f"bf16 dense sustained ({peak_src})",
-                "algorithmic": "4 N (N+1) S_up flops per slice (Hermitian upper triangle); "
-                               "hw_* counts the issued split-BF16 MMAs (3 products, 128-blocks)"}
-    else:
+
+    def time_form(method, sample_clocks):
+        for i in range(args.warmup):
+            step(i, method)
+        ctx.sync()
+        barrier()
+        ctx.set_profiling(True)
+        ctx.profile_read()
+        l0 = ctx.launches
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        times = []
+        sampler = ClockSampler(local) if sample_clocks else contextlib.nullcontext()
+        with sampler as clocks:
+            barrier()
+            ev0.record(stream)
+            for i in range(args.warmup, args.warmup + args.steps):
+                times.append(step(i, method))
+            ev1.record(stream)
+            barrier()
+        ms = ev0.elapsed_time(ev1)
+        ctx.sync()
+        kern_ms, kern_launches = ctx.profile_read()
+        ctx.set_profiling(False)
+        return dict(ms=max_over_ranks(ms, dev), kern_ms=kern_ms, kern_launches=kern_launches,
+                    launches=ctx.launches - l0, times=times,
+                    clocks=clocks.summary() if sample_clocks else None)
+
+    def roofline(method, r):
+        """Roofline of the contraction kernel of one timed form."""
+        s_up = [sources_up(w, t0 + k) for t0 in r["times"] for k in range(T_PER_STEP)]
+        herk_flops = sum(4.0 * N * (N + 1) * su * F for su in s_up)
+        kern_s = r["kern_ms"] / 1e3
+        if method in ("tc", "tc_fp16"):
+            ks, mmas = (16, 12) if method == "tc" else (32, 16)
+            chunk = tc_chunk(S, T_PER_STEP * F, tc_num_groups(N), num_sms)
+            stages = sum(sum(math.ceil(min(chunk, su - k0) / ks) for k0 in range(0, su, chunk))
+                         for su in s_up) * F
+            # tensor-pipe work in units of an M128 K16 BF16 MMA (an FP8 MMA
+            # of K = 32 takes the same time)
+            hw_flops = stages * mmas * 2 * 128 * 16 * sum(tc_groups(N))
+            peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
+            traffic_unit = TC_DRAM_BYTES_PER_UNIT.get(method)
+            units = sum(s_up) * F
+            return {"bound": "tensor", "achieved": herk_flops / kern_s / 1e12,
+                    "peak": peak, "unit": "TFLOP/s", "frac": herk_flops / kern_s / 1e12 / peak,
+                    "traffic": (traffic_unit * units / r["kern_launches"]) if traffic_unit else None,
+                    "kernel": "tc_vis_kernel", "launches": r["kern_launches"],
+                    "kernel_ms": r["kern_ms"],
+                    "hw_tflops": hw_flops / kern_s / 1e12,
+                    "hw_frac": hw_flops / kern_s / 1e12 / peak,
+                    "peak_kind": f"bf16 dense sustained ({peak_src})",
+                    "algorithmic": "4 N (N+1) S_up flops per slice (Hermitian upper triangle); "
+                                   "hw_* counts the issued MMAs in BF16 M128 K16 equivalents "
+                                   + ("(3 split-BF16 products, 128-blocks)" if method == "tc" else
+                                      "(FP16 hi product + 2 FP8 cross products, 128-blocks)")}
         peak = 152 * 128 * 2 * 1.92e9 / 1e12
-        roof = {"bound": "fp32-simt", "achieved": herk_flops / (kern_ms / 1e3) / 1e12,
-                "peak": peak, "unit": "TFLOP/s",
-                "frac": herk_flops / (kern_ms / 1e3) / 1e12 / peak, "traffic": None,
-                "kernel": "herk_plain_kernel", "launches": kern_launches, "kernel_ms": kern_ms}
+        return {"bound": "fp32-simt", "achieved": herk_flops / kern_s / 1e12, "peak": peak,
+                "unit": "TFLOP/s", "frac": herk_flops / kern_s / 1e12 / peak, "traffic": None,
+                "kernel": "herk_plain_kernel", "launches": r["kern_launches"],
+                "kernel_ms": r["kern_ms"]}
+
+    head = time_form(args.method, True)
+    ms = head["ms"]
+    value = job_rate(args.steps * vis_per_step, world, ms / 1e3)
+    clk = head["clocks"]
+    launches = head["launches"]
+    roof = roofline(args.method, head)
+    # the other fused form on the same steps
+    other = {"tc": "tc_fp16", "tc_fp16": "tc"}.get(args.method)
+    forms = {}
+    if other and not args.no_forms:
+        r = time_form(other, False)
+        forms[other] = {"value": job_rate(args.steps * vis_per_step, world, r["ms"] / 1e3),
+                        "ms_per_step": r["ms"] / args.steps, "gpu_launches": r["launches"],
+                        "roofline": roofline(other, r)}
 
     line = {
         "metric": "visibilities/s", "value": value, "unit": "vis/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "bf16" if args.method == "tc" else "fp32",
+        "dtype": {"tc": "bf16", "tc_fp16": "fp16+e4m3"}.get(args.method, "fp32"),
         "data": "synthetic (seeded); inputs larger than L2 (beam cubes "
                 f"{w['bm_cubes'].nbytes / 1e6:.0f} MB)",
         "method": args.method, "config": step_config(args, world),
-        "roofline": roof, "clocks": clk, "gpu_launches": launches,
+        "roofline": roof, "clocks": clk, "gpu_launches": launches, "forms": forms,
         # the reference returns the full N x N matrix (the metric above); the
         # distinct baselines a b >= a of it are N (N + 1) / 2 of those
         "unique_baselines_per_s": value * (N + 1) / (2.0 * N),
@@ -521,7 +544,7 @@ def run_ours(args):
                        "api": "hera_gpu_gb300.vis_gpu_multifreq -> hv_vis_multifreq"}
 
     # ---- the plain FP32 form on one step (the method of the reference) ----
-    if rank == 0 and not args.no_plain and args.method == "tc":
+    if rank == 0 and not args.no_plain and args.method != "plain":
         step(0, "plain")
         ctx.sync()
         ctx.set_profiling(True)
@@ -546,8 +569,8 @@ def run_ours(args):
     # all S sources, each form's output from a call of the timed shape (4
     # LSTs x all channels, the benchmark's own split-K chunking) -------------
     if rank == 0 and pool is not None:
-        methods = [args.method] + (["plain"] if not args.no_plain and args.method != "plain"
-                                   else [])
+        methods = [args.method] + list(forms) + (["plain"] if not args.no_plain and
+                                                 args.method != "plain" else [])
         corners = [(0, 0), (0, F - 1), (NTIMES - 1, 0), (NTIMES - 1, F - 1)]
         if args.no_corners:
             corners = corners[:1]
@@ -572,7 +595,7 @@ def run_ours(args):
         line["rel_err_vs_fp64"] = {
             **{m: max(e["err"] for e in errs[m]) for m in methods},
             "per_slice": errs,
-            "bound": {"tc": 1e-4, "plain": 1e-5},
+            "bound": {"tc": 1e-4, "tc_fp16": 1e-4, "plain": 1e-5},
             "sample": f"whole slices ({N} ant x {S} src) at (LST index, channel) "
                       f"{[(t, f) for t, f in corners]} of outputs of the timed call shape, against "
                       f"the FP64 oracle of the same inputs; the headline key is the largest"}
@@ -650,7 +673,7 @@ def run_configs(args, device, pool, cores):
     arr["bm_cubes"] = synth.beams_for(arr, dtype=np.float64)
     pub = synth.config_array(seed=3, nfreq=1, fmin=150e6, fmax=150e6, P=63, **PUBLISHED_SHAPE)
     pub["bm_cubes"] = synth.beams_for(pub, dtype=np.float64)
-    forms = [("plain", 1), ("tc", 1), ("plain", 2)]
+    forms = [("plain", 1), ("tc", 1), ("tc_fp16", 1), ("plain", 2)]
     plan = {"small": (small, 20, 3), "array": (arr, 3, 1), "published": (pub, 2, 1)}
     out = {}
     for name, (c, steps, warm) in plan.items():
@@ -676,19 +699,21 @@ def run_configs(args, device, pool, cores):
                                          host["bm"].shape[-1], o.data_ptr(), stream.cuda_stream)
             for _ in range(warm):
                 call()
+            torch.cuda.synchronize(dev)
             ctx.sync()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             for _ in range(n_steps):
                 call()
             e1.record(stream)
+            torch.cuda.synchronize(dev)
             ctx.sync()
             ms = e0.elapsed_time(e1) / n_steps
             t0 = time.perf_counter()
             V = vis_gpu(host["antpos"], freq, host["eq2tops"], host["crd_eq"], host["I_sky"],
                         host["bm"][0], precision=prec, method=method, context=ctx)
             e2e_s = time.perf_counter() - t0
-            key = f"{method}_fp{32 * prec}"
+            key = method if method.startswith("tc") else f"{method}_fp{32 * prec}"
             form = {"ms_per_call": ms, "vis_per_s": T * N * N / (ms / 1e3),
                     "e2e_vis_per_s": T * N * N / e2e_s, "steps": n_steps}
             if name == "published":

@@ -21,7 +21,7 @@ HV_ERR_CUDA = 3
 HV_ERR_TIMEOUT = 4
 HV_ERR_UNSUPPORTED = 5
 
-METHODS = {"auto": 0, "plain": 1, "tc": 2, "tc_bf16": 2}
+METHODS = {"auto": 0, "plain": 1, "tc": 2, "tc_bf16": 2, "tc_fp16": 3}
 
 class HvSim(ctypes.Structure):
     """hv_sim of include/heravis.h: one simulation of a batch (device
@@ -35,6 +35,9 @@ class HvSim(ctypes.Structure):
 
 HV_BATCH_GRAPH = 1
 HV_BATCH_AUTOTUNE = 2
+
+HV_TUNE_TEAM_WARPS = 1
+HV_TUNE_STAGES = 2
 
 # Every function of the ABI: name -> (restype, argtypes)
 _c_int, _c_void_p, _c_size_t, _c_double = ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_double
@@ -56,6 +59,7 @@ SIGNATURES = {
     "hv_set_profiling": (_c_int, [_c_void_p, _c_int]),
     "hv_profile_read": (_c_int, [_c_void_p, ctypes.POINTER(_c_double), ctypes.POINTER(ctypes.c_uint64)]),
     "hv_set_wait_limit": (_c_int, [_c_void_p, ctypes.c_uint64, _c_int]),
+    "hv_set_tuning": (_c_int, [_c_void_p, _c_int, _c_int]),
     "hv_median_filter": (_c_int, [_c_void_p, _PTR, _PTR, _c_int, _c_int, _c_int, _c_int, _c_int]),
     "hv_median_filter_device": (_c_int, [_c_void_p, _PTR, _PTR, _c_int, _c_int, _c_int, _c_int,
                                          _c_int, _c_void_p]),
@@ -222,6 +226,12 @@ class Context:
         ``stall`` the next fused launches are made to time out (fault
         injection for tests of failure detection)."""
         self.check(self.lib.hv_set_wait_limit(self.h, int(wait_s * 1e9), 1 if stall else 0))
+
+    def set_tuning(self, team_warps: int = 0, stages: int = 0):
+        """Launch shape of the fused kernel for later calls (hv_set_tuning;
+        0 = the default of each)."""
+        self.check(self.lib.hv_set_tuning(self.h, HV_TUNE_TEAM_WARPS, int(team_warps)))
+        self.check(self.lib.hv_set_tuning(self.h, HV_TUNE_STAGES, int(stages)))
 
     def median_filter(self, images, out, k0, k1):
         """Median filter of the (nimg, rows, cols) float32 images into out

@@ -56,12 +56,14 @@ struct hv_context {
   // injection (hv_set_wait_limit)
   uint64_t wait_ns = 0;
   int stall = 0;
+  // launch shape of the fused kernel (hv_set_tuning; zeros = defaults)
+  hv::TcTune tune{};
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
   // staging of host-API inputs / outputs
   DevBuf in_antpos, in_eq2tops, in_crd, in_I, in_bm, out_vis;
   // workspace
   DevBuf freqs, beamT, ucoef, rec, counts, blkcounts, v, partial, tcgroups;
-  DevBuf umax, sortkv, crd_sorted, I_sorted, tctable;
+  DevBuf umax, sortkv, crd_sorted, I_sorted, tctable, pixmax, sbound;
   HostBuf tctable_h;  // page-locked staging of the fused kernel's simulation table
   // page-locked blocks given back by destroyed batches, kept for the next
   // ones: freeing page-locked memory waits for the whole device
@@ -171,10 +173,12 @@ int check_shapes(hv_context* ctx, int precision, int method, int nant, int nfreq
                  int ntimes, int nsrc, int P) {
   if (precision != 1 && precision != 2)
     return fail(ctx, HV_ERR_ARG, "precision must be 1 or 2 (got %d)", precision);
-  if (method < HV_METHOD_AUTO || method > HV_METHOD_TC_BF16)
+  if (method < HV_METHOD_AUTO || method > HV_METHOD_TC_FP16)
     return fail(ctx, HV_ERR_ARG, "unknown method %d", method);
-  if (precision == 2 && method == HV_METHOD_TC_BF16)
-    return fail(ctx, HV_ERR_ARG, "the tensor-core method computes in FP32/BF16; use precision 1");
+  if (precision == 2 && (method == HV_METHOD_TC_BF16 || method == HV_METHOD_TC_FP16))
+    return fail(ctx, HV_ERR_ARG,
+                "the tensor-core methods compute in FP32 with BF16 or FP16/FP8 operands; use "
+                "precision 1");
   if (nant < 1) return fail(ctx, HV_ERR_ARG, "nant must be >= 1 (got %d)", nant);
   if (nant > 65536) return fail(ctx, HV_ERR_ARG, "nant %d too large", nant);
   if (nfreq < 1) return fail(ctx, HV_ERR_ARG, "nfreq must be >= 1 (got %d)", nfreq);
@@ -204,8 +208,9 @@ int run_device(hv_context* ctx, int method, const R* antpos, int nant, const dou
   if (ntimes == 0) return HV_OK;
   const int Np = ceil_div(nant, kAntPad) * kAntPad;
   const size_t PP = (size_t)P * P;
-  const bool tc = (method == HV_METHOD_TC_BF16) ||
+  const bool tc = (method == HV_METHOD_TC_BF16) || (method == HV_METHOD_TC_FP16) ||
                   (method == HV_METHOD_AUTO && sizeof(R) == 4);
+  const int form = method == HV_METHOD_TC_FP16 ? 1 : 0;
 
   HV_ENSURE(ctx->freqs, sizeof(double) * nfreq);
   HV_CK(cudaMemcpyAsync(ctx->freqs.p, freqs, sizeof(double) * nfreq, cudaMemcpyHostToDevice, st));
@@ -247,6 +252,14 @@ int run_device(hv_context* ctx, int method, const R* antpos, int nant, const dou
       HV_ENSURE(ctx->umax, sizeof(float) * (size_t)ntimes * nfreq);
       HV_LAUNCH(1, launch_ubound(ctx->ucoef.p, ntimes * nfreq, Np,
                                  static_cast<float*>(ctx->umax.p), st));
+      // FP16 + FP8 form: the beam's largest value per pixel, for the slices'
+      // scales
+      if (form == 1) {
+        HV_ENSURE(ctx->pixmax, sizeof(float) * (size_t)nfreq * PP);
+        HV_ENSURE(ctx->sbound, sizeof(float) * (size_t)ntimes * nfreq);
+        HV_LAUNCH(1, launch_beam_pixmax(reinterpret_cast<const float*>(beamT), nfreq, P, Np,
+                                        static_cast<float*>(ctx->pixmax.p), st));
+      }
       const R* crd_use = crd_eq;
       const R* I_use = I_sky;
       if (nsrc > 0) {
@@ -268,7 +281,17 @@ int run_device(hv_context* ctx, int method, const R* antpos, int nant, const dou
                                             static_cast<int*>(ctx->blkcounts.p), ctx->rec.p,
                                             rec_stride, counts + t0, st));
         HV_LAUNCH(1, launch_tc_relative(ctx->rec.p, rec_stride, counts + t0, nt, nsrc, st));
+        float* sbound = nullptr;
+        if (form == 1) {
+          sbound = static_cast<float*>(ctx->sbound.p) + (size_t)t0 * nfreq;
+          HV_LAUNCH(1, launch_slice_bound(ctx->rec.p, rec_stride, counts + t0, nt, nsrc,
+                                          static_cast<const float*>(ctx->pixmax.p), nfreq, P,
+                                          sbound, st));
+        }
         TcSimDesc L{};
+        L.sbound = sbound;
+        L.form = form;
+        L.tune = ctx->tune;
         L.counts = counts + t0;
         L.U = static_cast<const U*>(ctx->ucoef.p) + (size_t)t0 * nfreq * Np;
         L.beamT = reinterpret_cast<const float*>(beamT);
@@ -465,7 +488,8 @@ int hv_destroy(hv_context* ctx) {
   DevBuf* bufs[] = {&ctx->in_antpos, &ctx->in_eq2tops, &ctx->in_crd, &ctx->in_I, &ctx->in_bm,
                     &ctx->out_vis, &ctx->freqs, &ctx->beamT, &ctx->ucoef, &ctx->rec,
                     &ctx->counts, &ctx->blkcounts, &ctx->v, &ctx->partial, &ctx->tcgroups,
-                    &ctx->umax, &ctx->sortkv, &ctx->crd_sorted, &ctx->I_sorted, &ctx->tctable};
+                    &ctx->umax, &ctx->sortkv, &ctx->crd_sorted, &ctx->I_sorted, &ctx->tctable,
+                    &ctx->pixmax, &ctx->sbound};
   for (DevBuf* b : bufs) release(ctx, *b);
   if (ctx->tctable_h.p) cudaFreeHost(ctx->tctable_h.p);
   for (auto& hp : ctx->host_pool) cudaFreeHost(hp.first);
@@ -563,6 +587,24 @@ int hv_set_profiling(hv_context* ctx, int enable) {
   if (!ctx) return HV_ERR_ARG;
   ctx->profiling = enable != 0;
   return HV_OK;
+}
+
+int hv_set_tuning(hv_context* ctx, int param, int value) {
+  if (!ctx) return HV_ERR_ARG;
+  switch (param) {
+    case HV_TUNE_TEAM_WARPS:
+      if (value != 0 && value != 8 && value != 16)
+        return fail(ctx, HV_ERR_ARG, "team warps must be 0, 8 or 16 (got %d)", value);
+      ctx->tune.team_warps = value;
+      return HV_OK;
+    case HV_TUNE_STAGES:
+      if (value != 0 && (value < 2 || value > 8))
+        return fail(ctx, HV_ERR_ARG, "stages must be 0 or in [2, 8] (got %d)", value);
+      ctx->tune.stages = value;
+      return HV_OK;
+    default:
+      return fail(ctx, HV_ERR_ARG, "unknown tuning parameter %d", param);
+  }
 }
 
 int hv_set_wait_limit(hv_context* ctx, uint64_t wait_ns, int stall) {

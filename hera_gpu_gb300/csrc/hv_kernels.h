@@ -58,6 +58,16 @@ cudaError_t launch_prep_strided(const R* crd_eq, const R* I_sky, int nsrc, const
 cudaError_t launch_tc_relative(void* rec, size_t rec_stride, const int* counts, int nt, int nsrc,
                                cudaStream_t st);
 
+// FP16 + FP8 form: pixmax[f][pix] = max over antennas of |beamT[f][pix][a]|
+// (nfreq * P * P floats).
+cudaError_t launch_beam_pixmax(const float* beamT, int nfreq, int P, int Np, float* pixmax,
+                               cudaStream_t st);
+// FP16 + FP8 form: sbound[tt * nf + f] (zeroed here) = a bound of |A| sqrt(I)
+// over the records of time tt at frequency f, for the nt times of rec.
+cudaError_t launch_slice_bound(const void* rec, size_t rec_stride, const int* counts, int nt,
+                               int nsrc, const float* pixmax, int nf, int P, float* sbound,
+                               cudaStream_t st);
+
 // --- hv_plain.cu -----------------------------------------------------------
 // Source chunk of the split-K sum over sources (plain path).
 constexpr int kPlainChunk = 4096;
@@ -85,12 +95,18 @@ cudaError_t launch_reduce(const R* partial, size_t slice_stride, const int* coun
                           cudaStream_t st);
 
 // --- hv_tc.cu --------------------------------------------------------------
+// Launch shape of the fused kernel; 0 everywhere = the defaults.
+struct TcTune {
+  int team_warps;  // 16: one generator team of 16 warps per stage (FP16 + FP8 cluster launches)
+  int stages;      // cap on the operand stages in shared memory (>= 2)
+};
 // One simulation of a fused-kernel launch (device pointers).
 struct TcSimDesc {
   const int* counts;    // [nt] sources above the horizon per time
   const void* U;        // Ucoef32 [nt][nf][Np]
   const float* beamT;   // [nf][P*P][Np]
   const float* umax;    // [nt * nf] bound of |U|_1 per slice (launch_ubound)
+  const float* sbound;  // [nt * nf] bound of |A| sqrt(I) per slice (form 1; launch_slice_bound)
   float* partial;       // [nt * nf][ceil(nsrc / chunk)][2][Np][Np]
   const void* groups;   // device group table (tc_fill_group_table for this nant)
   int ngroups, max_slots;
@@ -98,6 +114,8 @@ struct TcSimDesc {
   int rec_stride;       // records per time, a multiple of 32 >= nsrc
   int nt, nf, Np, nant, P, nsrc;
   int chunk;            // sources per split-K chunk (multiple of 32)
+  int form;             // 0: split BF16; 1: FP16 + FP8 (needs sbound)
+  TcTune tune;          // launch shape (the first simulation's applies to a launch)
 };
 size_t tc_sim_table_bytes(int nsims);
 int tc_num_groups(int nant);

@@ -326,6 +326,92 @@ cudaError_t launch_tc_relative(void* rec, size_t rec_stride, const int* counts, 
   return cudaGetLastError();
 }
 
+// ---------------------------------------- FP16 + FP8 form: slice bounds --
+// pixmax[f][pix] = max over antennas of |beamT[f][pix][a]|: one warp per
+// (frequency, pixel) row of the transposed beam.
+__global__ void __launch_bounds__(256)
+beam_pixmax_kernel(const float* __restrict__ beamT, long long rows, int Np,
+                   float* __restrict__ pixmax) {
+  const int lane = threadIdx.x & 31;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows; r += nw) {
+    const float* row = beamT + r * Np;
+    float m = 0.f;
+    for (int a = lane; a < Np; a += 32) m = fmaxf(m, fabsf(row[a]));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) pixmax[r] = m;
+  }
+}
+
+cudaError_t launch_beam_pixmax(const float* beamT, int nfreq, int P, int Np, float* pixmax,
+                               cudaStream_t st) {
+  const long long rows = (long long)nfreq * P * P;
+  const long long blocks = std::min<long long>(4096, (rows + 7) / 8);
+  beam_pixmax_kernel<<<(int)std::max<long long>(blocks, 1), 256, 0, st>>>(beamT, rows, Np,
+                                                                          pixmax);
+  return cudaGetLastError();
+}
+
+// sbound[tt][f] = max over the records of time tt of sqrt(I) x the largest
+// |beam| over antennas at the record's four beam corners: a bound of |A|
+// sqrt(I) over the slice (bilinear weights lie in [0, 1]).  Each thread
+// holds up to kBoundRecs records; per frequency a warp reduces and one lane
+// raises the slice's bound (float bits of non-negative values order as
+// unsigned integers).  sbound must be zero beforehand.
+constexpr int kBoundRecs = 4;
+__global__ void __launch_bounds__(256)
+slice_bound_kernel(const SrcRec32* __restrict__ rec, size_t rec_stride,
+                   const int* __restrict__ counts, const float* __restrict__ pixmax, int nf,
+                   int PP, int dx, int dy, unsigned* __restrict__ sbound) {
+  const int tt = blockIdx.y;
+  const int n = counts[tt];
+  const SrcRec32* r = rec + (size_t)tt * rec_stride;
+  for (long long base = (long long)blockIdx.x * blockDim.x * kBoundRecs; base < n;
+       base += (long long)gridDim.x * blockDim.x * kBoundRecs) {
+    int pix[kBoundRecs];
+    float amp[kBoundRecs];
+#pragma unroll
+    for (int k = 0; k < kBoundRecs; ++k) {
+      const long long i = base + (long long)k * blockDim.x + threadIdx.x;
+      pix[k] = 0;
+      amp[k] = 0.f;
+      if (i < n) {
+        pix[k] = r[i].pix;
+        amp[k] = fabsf(r[i].amp);
+      }
+    }
+    for (int f = 0; f < nf; ++f) {
+      const float* pm = pixmax + (size_t)f * PP;
+      float m = 0.f;
+#pragma unroll
+      for (int k = 0; k < kBoundRecs; ++k) {
+        if (amp[k] == 0.f) continue;
+        const int q = pix[k];
+        const float c = fmaxf(fmaxf(__ldg(pm + q), __ldg(pm + q + dx)),
+                              fmaxf(__ldg(pm + q + dy), __ldg(pm + q + dx + dy)));
+        m = fmaxf(m, amp[k] * c);
+      }
+      for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+      if ((threadIdx.x & 31) == 0 && m > 0.f)
+        atomicMax(sbound + (size_t)tt * nf + f, __float_as_uint(m));
+    }
+  }
+}
+
+cudaError_t launch_slice_bound(const void* rec, size_t rec_stride, const int* counts, int nt,
+                               int nsrc, const float* pixmax, int nf, int P, float* sbound,
+                               cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(sbound, 0, sizeof(float) * (size_t)nt * nf, st);
+  if (e != cudaSuccess) return e;
+  const int per_block = 256 * kBoundRecs;
+  const int blocks = std::max(1, std::min(ceil_div(std::max(nsrc, 1), per_block), 1024));
+  dim3 grid(blocks, nt);
+  slice_bound_kernel<<<grid, 256, 0, st>>>(static_cast<const SrcRec32*>(rec), rec_stride, counts,
+                                           pixmax, nf, P * P, P > 1 ? 1 : 0, P > 1 ? P : 0,
+                                           reinterpret_cast<unsigned*>(sbound));
+  return cudaGetLastError();
+}
+
 template cudaError_t launch_beam_transpose<float>(const float*, int, int, int, int, float*, cudaStream_t);
 template cudaError_t launch_beam_transpose<double>(const double*, int, int, int, int, double*, cudaStream_t);
 template cudaError_t launch_ucoef<float>(const float*, int, int, const float*, int, int, const double*, int, void*, cudaStream_t);

@@ -47,12 +47,32 @@
 //   (V[a,b] = sum_s v_a conj(v_b)); the minus sign is the instruction
 //   descriptor's negate-A bit.  Split BF16 keeps hi*hi + hi*lo + lo*hi.
 //
+// Second form (kForm = 1, HV_METHOD_TC_FP16): FP16 hi parts and FP8 (E4M3)
+// cross terms.  Per (time, frequency) slice the phasors are scaled by a power
+// of two c so that |X| = |c v| <= 256 (c from a bound of the slice's largest
+// |A| sqrt(I), tc_slice_bound_kernel), and split X = H + L with H the FP16
+// rounding of X (11 significant bits) and L = X - H exact in FP32.  Then
+//   X_a conj(X_b) ~ H_a conj(H_b) + e4m3(X_a) conj(e4m3(L_b))
+//                                 + e4m3(L_a) conj(e4m3(X_b)),
+// the first product on kind::f16, the two cross terms on kind::f8f6f4 (FP8
+// runs at twice the FP16 rate), all into the same FP32 accumulators; the
+// epilogue multiplies by 1/c^2 (exact).  A stage is 32 sources, with two
+// tiles per slot (16 KB each, 128-byte rows):
+//   FP16 tile  [Re H s0-31 | Im H s0-31]                  (64 B + 64 B)
+//   FP8 tile   [Re X8 | Im X8 | Re L8 | Im L8], s0-31 each  (4 x 32 B)
+// and 16 MMAs per group and stage (8 FP16 of K = 16, 8 FP8 of K = 32): the
+// tensor-pipe time of 8 K = 16 BF16 MMAs per 16 sources, against 12 for
+// split BF16.  Operand rounding costs about 1e-5 of relative error (3-bit
+// mantissas on terms 2^-11 of the product).
+//
 // Every wait on an mbarrier is bounded in time; on expiry the kernel raises
 // an error flag, lets in-flight copies and MMAs land (again bounded), frees
 // TMEM and returns, so the host sees HV_ERR_TIMEOUT instead of a hung GPU.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_fp8.h>
 
 #include <algorithm>
 #include <vector>
@@ -63,9 +83,18 @@
 namespace hv {
 
 constexpr int TC_ROWS = 128;          // antennas per block = MMA M
-constexpr int TC_KS = 16;             // sources per stage
-constexpr int TC_SLOT = 16384;        // one block's tile per stage: 128 rows x 128 B (hi and lo)
-constexpr int TC_REC = TC_KS * 32;    // bytes of source records per stage
+constexpr int TC_SLOT = 16384;        // one operand tile: 128 rows x 128 B
+// Sources per stage: 16 for split BF16 (one tile per slot: hi and lo of 16
+// sources), 32 for FP16 + FP8 (two tiles per slot, see above).
+template <int kForm> struct TcForm;
+template <> struct TcForm<0> {
+  static constexpr int KS = 16, TILES = 1;
+};
+template <> struct TcForm<1> {
+  static constexpr int KS = 32, TILES = 2;
+};
+constexpr int TC_KS_MAX = 32;
+constexpr int TC_REC_MAX = TC_KS_MAX * 32;  // bytes of source records per stage (largest form)
 // Record stages: more than operand stages (they are small), so the TMA
 // producer runs further ahead and a generator warp finds its next records
 // loaded even while slower warps still hold earlier stages.
@@ -77,17 +106,19 @@ constexpr int TC_GEN_THREADS = TC_GEN_WARPS * 32;
 // their rows, so that 4 (8) stages are generated at once.
 constexpr int TC_TEAM_WARPS = 8;
 constexpr int TC_MAX_STAGES = 8;
-// Stages accumulated in TMEM before the sum is added to the item's split-K
+// Sources accumulated in TMEM before the sum is added to the item's split-K
 // partial in global memory (FP32, round to nearest) and the accumulator
 // starts again.  The tensor core's accumulation into TMEM loses a fraction
 // of an ulp of the accumulated value per addition, always toward zero, so
 // its error grows with the number of additions into one value: measured
 // against the FP64 oracle at 350 antennas x 1M sources, the relative error
 // of an autocorrelation summed over 16384 sources is -1e-4, over 1024
-// sources -1.3e-5.  TC_FLUSH_STAGES x TC_KS sources per flush bound it.
-#ifndef TC_FLUSH_STAGES
-#define TC_FLUSH_STAGES 128
+// sources -1.3e-5.  TC_FLUSH_SOURCES (a multiple of every stage size) per
+// flush bound it.
+#ifndef TC_FLUSH_SOURCES
+#define TC_FLUSH_SOURCES 2048
 #endif
+static_assert(TC_FLUSH_SOURCES % TC_KS_MAX == 0, "flush interval: whole stages of every form");
 constexpr int TC_PRODUCER_WARP = TC_GEN_WARPS;
 constexpr int TC_MMA_WARP = TC_GEN_WARPS + 1;
 constexpr int TC_PUSH_WARP = TC_GEN_WARPS + 2;  // cluster mode: pushes tiles to peer CTAs
@@ -118,7 +149,6 @@ struct TcGroup {
   int dst_rank[3][TC_MAX_CLUSTER - 1];
   int dst_slot[3][TC_MAX_CLUSTER - 1];
   int recv_slots;                      // slots pushed here by peers per stage
-  int full_count;                      // arrivals per stage on this CTA's smem_full
   int empty_count;                     // arrivals per stage on this CTA's smem_empty
   int commit_mask;                     // CTAs this CTA's MMA completion is signalled to
   int write_mask;                      // CTAs this CTA's generators write to (bit = rank)
@@ -131,6 +161,7 @@ struct TcSim {
   const Ucoef32* U;       // [nt][nf][Np]
   const float* beamT;     // [nf][PP][Np]
   const float* umax;      // [nt * nf] bound of |U|_1 per slice
+  const float* sbound;    // [nt * nf] bound of |A| sqrt(I) per slice (FP16 + FP8 form)
   float* partial;         // [nt * nf][nchunk][2][Np][Np]
   const TcGroup* groups;  // [ngroups]
   long long item0;        // first item of this simulation in the launch
@@ -158,7 +189,7 @@ struct TcParams {
   // cluster fits on runs the group items [*split * ngroups, total_items).
   const int* split;
   int split_side;  // 0: the cluster launch, 1: the one-CTA launch
-  int team_warps;  // generator warps per stage (8, or 4 / 2 for small one-slot groups)
+  int team_warps;  // generator warps per stage without clusters (8, or 4 / 2 for small groups)
 };
 
 // Read-only load of a pointer-valued field.
@@ -349,14 +380,18 @@ __device__ __forceinline__ uint32_t desc_lo(uint32_t saddr) {
   return ((saddr & 0x3FFFFu) >> 4) | (1u << 16);
 }
 
-// Instruction descriptor, kind::f16: D F32, A and B BF16, both K-major,
-// M = 128, N = n.
-__device__ __forceinline__ uint32_t idesc_bf16(int n, bool negate_a) {
-  uint32_t d = (1u << 4) | (1u << 7) | (1u << 10);
+// Instruction descriptor: D F32, A and B K-major, M = 128, N = n; the A/B
+// type code is 1 for BF16 (kind::f16) and 0 for FP16 (kind::f16) or E4M3
+// (kind::f8f6f4).
+__device__ __forceinline__ uint32_t idesc_mma(int n, bool negate_a, uint32_t ab_type) {
+  uint32_t d = (1u << 4) | (ab_type << 7) | (ab_type << 10);
   d |= (uint32_t)(n >> 3) << 17;
   d |= (uint32_t)(TC_ROWS >> 4) << 24;
   if (negate_a) d |= 1u << 13;
   return d;
+}
+__device__ __forceinline__ uint32_t idesc_bf16(int n, bool negate_a) {
+  return idesc_mma(n, negate_a, 1u);
 }
 
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint32_t a_lo, uint32_t b_lo,
@@ -387,6 +422,44 @@ __device__ __forceinline__ void issue_group(uint32_t d_re, uint32_t a, uint32_t 
     mma_bf16(d_re, aa + 2u, bb + 2u, idp, 1u);   // Im Im
     mma_bf16(d_im, aa + 2u, bb, idp, acc);       // Im Re
     mma_bf16(d_im, aa, bb + 2u, idn, 1u);        // -Re Im
+  }
+}
+
+// kind::f8f6f4 with E4M3 operands (K = 32 per instruction).
+__device__ __forceinline__ void mma_e4m3(uint32_t d_tmem, uint32_t a_lo, uint32_t b_lo,
+                                         uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n .reg .b64 da, db;\n setp.ne.b32 p, %5, 0;\n"
+      " mov.b64 da, {%1, %3};\n mov.b64 db, {%2, %3};\n"
+      " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], da, db, %4, p;\n}\n" ::"r"(d_tmem),
+      "r"(a_lo), "r"(b_lo), "r"(kDescHi), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// The 16 MMAs of one group and one 32-source stage of the FP16 + FP8 form.
+// a16/b16: descriptor low words of the row block's and the column blocks'
+// FP16 tiles (K chunks of 32 bytes: Re s0-15, Re s16-31, Im s0-15, Im s16-31
+// at +0, +2, +4, +6); a8/b8: the FP8 tiles (Re X8, Im X8, Re L8, Im L8 at
+// +0, +2, +4, +6).  The FP16 and E4M3 instruction descriptors coincide.
+__device__ __forceinline__ void issue_group_f16f8(uint32_t d_re, uint32_t a16, uint32_t b16,
+                                                  uint32_t a8, uint32_t b8, uint32_t idp,
+                                                  uint32_t idn, bool first) {
+  const uint32_t d_im = d_re + 256;
+#pragma unroll
+  for (uint32_t h = 0; h < 4; h += 2) {  // source halves s0-15, s16-31
+    const uint32_t acc = (first && h == 0) ? 0u : 1u;
+    mma_bf16(d_re, a16 + h, b16 + h, idp, acc);              // Re Re
+    mma_bf16(d_re, a16 + 4u + h, b16 + 4u + h, idp, 1u);     // Im Im
+    mma_bf16(d_im, a16 + 4u + h, b16 + h, idp, acc);         // Im Re
+    mma_bf16(d_im, a16 + h, b16 + 4u + h, idn, 1u);          // -Re Im
+  }
+#pragma unroll
+  for (int pr = 0; pr < 2; ++pr) {  // X8 (a) x L8 (b), then L8 (a) x X8 (b)
+    const uint32_t xa = pr == 0 ? 0u : 4u, yb = pr == 0 ? 4u : 0u;
+    mma_e4m3(d_re, a8 + xa, b8 + yb, idp, 1u);               // Re Re
+    mma_e4m3(d_re, a8 + xa + 2u, b8 + yb + 2u, idp, 1u);     // Im Im
+    mma_e4m3(d_im, a8 + xa + 2u, b8 + yb, idp, 1u);          // Im Re
+    mma_e4m3(d_im, a8 + xa, b8 + yb + 2u, idn, 1u);          // -Re Im
   }
 }
 
@@ -422,6 +495,10 @@ __device__ __forceinline__ void red_add4(float4* p, float4 v) {
   asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(v.x), "f"(v.y),
                "f"(v.z), "f"(v.w)
                : "memory");
+}
+
+__device__ __forceinline__ void sts64(uint32_t addr, uint2 v) {
+  asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(addr), "r"(v.x), "r"(v.y) : "memory");
 }
 
 __device__ __forceinline__ void sts128(uint32_t addr, uint4 v) {
@@ -471,6 +548,42 @@ __device__ __forceinline__ void split_pack(const float* v, uint4& hi, uint4& lo)
   lo = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
+// Eight scaled phasor parts X -> their FP16 roundings H (packed in pairs,
+// lower K index in the low half-word), and the E4M3 roundings (saturating)
+// of X and of L = X - H (exact in FP32), packed four to a word.
+__device__ __forceinline__ void split_f16_e4m3(const float* x, uint4& h16, uint2& x8,
+                                               uint2& l8) {
+  uint32_t h[4];
+  uint32_t px[4], pl[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const __half2 hh = __floats2half2_rn(x[2 * i], x[2 * i + 1]);
+    h[i] = *reinterpret_cast<const uint32_t*>(&hh);
+    const float2 hf = __half22float2(hh);
+    px[i] = __nv_cvt_float2_to_fp8x2(make_float2(x[2 * i], x[2 * i + 1]), __NV_SATFINITE,
+                                     __NV_E4M3);
+    pl[i] = __nv_cvt_float2_to_fp8x2(make_float2(x[2 * i] - hf.x, x[2 * i + 1] - hf.y),
+                                     __NV_SATFINITE, __NV_E4M3);
+  }
+  h16 = make_uint4(h[0], h[1], h[2], h[3]);
+  x8 = make_uint2(__byte_perm(px[0], px[1], 0x5410), __byte_perm(px[2], px[3], 0x5410));
+  l8 = make_uint2(__byte_perm(pl[0], pl[1], 0x5410), __byte_perm(pl[2], pl[3], 0x5410));
+}
+
+// Scale of a slice of the FP16 + FP8 form: c = 2^k with c * bound <= 256
+// (bound: the slice's largest |A| sqrt(I), or a bound of it), and 1 / c^2.
+__device__ __forceinline__ void slice_scale(float bound, float& c, float& inv_c2) {
+  int e = 0;  // bound <= 2^e
+  const uint32_t b = __float_as_uint(bound);
+  const int ex = (int)((b >> 23) & 0xffu);
+  if (bound > 0.f && ex < 255) {
+    e = ex == 0 ? -126 : ex - 127 + ((b & 0x7fffffu) ? 1 : 0);
+  }
+  const int k = max(-60, min(60, 8 - e));
+  c = __uint_as_float((uint32_t)(127 + k) << 23);
+  inv_c2 = __uint_as_float((uint32_t)(127 - 2 * k) << 23);
+}
+
 // Phasors of 8 consecutive records (one unit) for one antenna: v = A sqrt(I)
 // e^{2 pi i phi}.  Record 0's direction is the unit's reference; its pad word
 // holds the largest |s - s_ref|_1 of the unit (tc_relative_kernel), its sign
@@ -487,7 +600,8 @@ __device__ __forceinline__ void split_pack(const float* v, uint4& hi, uint4& lo)
 template <bool kNear, bool kOnePixel>
 __device__ __forceinline__ void gen_unit_path(const SrcRec32* rec, const Ucoef32& uc,
                                               const float* beam_a, int Np, int dx, int dy,
-                                              float4 ref, float ph_ref, float* rv, float* iv) {
+                                              float4 ref, float ph_ref, float csc, float* rv,
+                                              float* iv) {
   float c00 = 0.f, c01 = 0.f, c10 = 0.f, c11 = 0.f;
   if (kOnePixel) {
     const float* bp = beam_a + (size_t)__float_as_int(reinterpret_cast<const float4*>(rec)[1].x) * Np;
@@ -524,15 +638,16 @@ __device__ __forceinline__ void gen_unit_path(const SrcRec32* rec, const Ucoef32
     // BF16 operands
     float sn, cs;
     __sincosf(6.28318530717958648f * ph, &sn, &cs);
-    const float amp = A * ra.w;
+    const float amp = A * (ra.w * csc);
     rv[q] = amp * cs;
     iv[q] = amp * sn;
   }
 }
 
+// csc: the slice's scale (1 for split BF16; a power of two, so exact).
 __device__ __forceinline__ void gen_unit(const SrcRec32* rec, const Ucoef32& uc,
                                          const float* beam_a, int Np, int dx, int dy, float dlim,
-                                         float* rv, float* iv) {
+                                         float csc, float* rv, float* iv) {
   const float4* rp0 = reinterpret_cast<const float4*>(rec);
   const float4 q0a = rp0[0], q0b = rp0[1];
   const int flags = __float_as_int(q0b.w);
@@ -540,10 +655,10 @@ __device__ __forceinline__ void gen_unit(const SrcRec32* rec, const Ucoef32& uc,
   const bool near = __int_as_float(flags & 0x7fffffff) <= dlim;
   if (near) {
     const float ph_ref = phase_exact(uc, q0a.x, q0a.y, q0a.z);
-    if (one_pixel) gen_unit_path<true, true>(rec, uc, beam_a, Np, dx, dy, q0a, ph_ref, rv, iv);
-    else gen_unit_path<true, false>(rec, uc, beam_a, Np, dx, dy, q0a, ph_ref, rv, iv);
+    if (one_pixel) gen_unit_path<true, true>(rec, uc, beam_a, Np, dx, dy, q0a, ph_ref, csc, rv, iv);
+    else gen_unit_path<true, false>(rec, uc, beam_a, Np, dx, dy, q0a, ph_ref, csc, rv, iv);
   } else {
-    gen_unit_path<false, false>(rec, uc, beam_a, Np, dx, dy, q0a, 0.f, rv, iv);
+    gen_unit_path<false, false>(rec, uc, beam_a, Np, dx, dy, q0a, 0.f, csc, rv, iv);
   }
 }
 
@@ -561,7 +676,7 @@ struct ItemInfo {
 #define SIM_I(d, f) (kTable ? __ldg(&(d).sim->f) : p.one.f)
 #define SIM_P(d, f) (kTable ? ldg_ptr(&(d).sim->f) : p.one.f)
 
-template <bool kCluster, bool kTable>
+template <bool kCluster, bool kTable, int kKS>
 __device__ __forceinline__ bool decode_item(const TcParams& p, long long it, int rank,
                                             ItemInfo& d) {
   long long rest = it;
@@ -603,24 +718,37 @@ __device__ __forceinline__ bool decode_item(const TcParams& p, long long it, int
   d.sl = t * nf + d.f;
   d.s0 = d.k * chunk;
   d.s1 = min(d.s0 + chunk, cnt);
-  d.nst = (d.s1 - d.s0 + TC_KS - 1) / TC_KS;
+  d.nst = (d.s1 - d.s0 + kKS - 1) / kKS;
   return true;
 }
 
 // 19 warps on 4 schedulers: the busiest scheduler holds 5 warps, and its
 // 16K-register file caps a thread at 96 registers (launch bounds give that).
-template <bool kCluster, bool kTable>
+// kTeam16 (FP16 + FP8 form): one team of 16 generator warps per stage in
+// cluster mode, instead of two teams of 8 taking alternate stages.
+template <bool kCluster, bool kTable, int kForm, bool kTeam16 = false>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant__ TcParams p) {
+  constexpr int KS = TcForm<kForm>::KS;         // sources per stage
+  constexpr int TILES = TcForm<kForm>::TILES;   // tiles per slot per stage
+  constexpr int REC = KS * 32;                  // record bytes per stage
+  constexpr int FLUSH = TC_FLUSH_SOURCES / KS;  // stages per accumulator flush
+  // generator warps per stage in cluster mode (compile-time there; launches
+  // without clusters take theirs from the parameters)
+  constexpr int CL_TEAM = kTeam16 ? 16 : TC_TEAM_WARPS;
+  static_assert(!kTeam16 || (kForm == 1 && kCluster), "16-warp teams: FP16 + FP8 cluster launches");
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
   const int NS = p.nstages;
   const uint32_t op_base = smem_u32(smem);
-  const uint32_t stage_bytes = (uint32_t)p.max_slots * TC_SLOT;
+  // a stage: the FP16 / split-BF16 tiles of every slot side by side, then
+  // (FP16 + FP8 form) the FP8 tiles of every slot side by side
+  const uint32_t tile8_off = (uint32_t)p.max_slots * TC_SLOT;
+  const uint32_t stage_bytes = (uint32_t)TILES * tile8_off;
   uint8_t* rec_smem = smem + (size_t)NS * stage_bytes;
   const uint32_t rec_base = smem_u32(rec_smem);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(rec_smem + (size_t)TC_NREC * TC_REC);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(rec_smem + (size_t)TC_NREC * REC);
   const uint32_t bar0 = smem_u32(bars);
   // barrier addresses
   // record stages r < TC_NREC, operand stages s < NS
@@ -651,18 +779,26 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
   }
   const TcGroup* mine = (kTable ? ldg_ptr(&p.sims[0].groups) : p.one.groups) + rank;
   // cluster mode: operand bytes this CTA receives from peers per stage
-  const uint32_t recv_bytes = kCluster ? (uint32_t)__ldg(&mine->recv_slots) * TC_SLOT : 0u;
+  const uint32_t recv_bytes =
+      kCluster ? (uint32_t)__ldg(&mine->recv_slots) * (uint32_t)(TILES * TC_SLOT) : 0u;
+  // cluster mode: does this CTA generate any block?
+  const int nown = kCluster ? __ldg(&mine->nown) : 0;
+  const bool generates = !kCluster || nown > 0;
   if (threadIdx.x == 0) {
-    const int full_count = kCluster ? mine->full_count : p.team_warps;
+    // arrivals per stage on smem_full: one per generator warp of the team
+    // (if this CTA generates) and, in cluster mode, the MMA thread's arming
+    // of the bytes its peers push
+    const int team_warps = kCluster ? CL_TEAM : p.team_warps;
+    const int full_count = (generates ? team_warps : 0) + (recv_bytes ? 1 : 0);
     const int empty_count = kCluster ? mine->empty_count : 1;
     for (int r = 0; r < TC_NREC; ++r) {
       mbar_init(rec_full(r), 1);
-      mbar_init(rec_empty(r), p.team_warps);
+      mbar_init(rec_empty(r), team_warps);
     }
     for (int s = 0; s < NS; ++s) {
       mbar_init(smem_full(s), full_count);
       mbar_init(smem_empty(s), empty_count);
-      mbar_init(gen_done(s), p.team_warps);
+      mbar_init(gen_done(s), team_warps);
     }
     mbar_init(acc_full, 1);
     mbar_init(acc_empty, TC_GEN_THREADS);
@@ -686,20 +822,17 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
   if (kCluster) cluster_sync_all();
   tc_fence_after();
   const uint32_t tmem = *tmem_holder;
-  // cluster mode: does this CTA generate any block?
-  const int nown = kCluster ? __ldg(&mine->nown) : 0;
-  const bool generates = !kCluster || nown > 0;
 
   if (warp < TC_GEN_WARPS) {
     // ------------------------------------------------ phasor generators --
     const int tid = threadIdx.x;
-    const int team_warps = kCluster ? TC_TEAM_WARPS : p.team_warps;
+    const int team_warps = kCluster ? CL_TEAM : p.team_warps;
     const int nteams = TC_GEN_WARPS / team_warps;
     const int team = warp / team_warps;  // takes the stages with gs % nteams == team
     uint32_t gs = 0, ic = 0;
     ItemInfo d;
     for (long long it = it0; it < it_end; it += istep) {
-      if (!decode_item<kCluster, kTable>(p, it, rank, d)) continue;
+      if (!decode_item<kCluster, kTable, KS>(p, it, rank, d)) continue;
       const TcGroup* gp = SIM_P(d, groups) + d.g;
       const int Np = SIM_I(d, Np), dx = SIM_I(d, dx), dy = SIM_I(d, dy);
       const int g_nslots = __ldg(&gp->nslots), g_npairs = __ldg(&gp->npairs);
@@ -712,13 +845,22 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       if (umax_sl >= 4.0e6f && tid == 0) atomicExch(p.err, kErrRange);
       const float dlim = 32.0f / fmaxf(umax_sl, 1e-30f);
       const float* beam = SIM_P(d, beamT) + (size_t)d.f * SIM_I(d, PP) * Np;
+      // the slice's scale (FP16 + FP8 form)
+      float csc = 1.f, inv_c2 = 1.f;
+      if (kForm == 1) slice_scale(__ldg(SIM_P(d, sbound) + d.sl), csc, inv_c2);
       // the slots this CTA fills: all of its group's (no clusters) or the
       // ones it owns (cluster mode)
       const int nfill = kCluster ? nown : g_nslots;
-      // this thread's units (fixed for the item): antenna row `row` and
-      // sources 8 sg .. 8 sg + 7 of its team's stages, in each slot it fills
+      // this thread's units (fixed for the item): antenna row `row` and the
+      // units of 8 sources [sg * upt, sg * upt + upt) of its team's stages,
+      // in each slot it fills
+      // a team covers its rows (128, or fewer for the small teams of
+      // one-slot launches) with 2 thread groups along the stage, or 4 for a
+      // team of 16
+      constexpr int NSG = kTeam16 ? 4 : 2;
+      constexpr int UPT = (KS / 8) / NSG;  // units per thread per stage
       const int tt = tid & (team_warps * 32 - 1);
-      const int nrows = team_warps * 16;  // rows a team covers (the block's valid rows)
+      const int nrows = kCluster ? TC_ROWS : team_warps * 16;
       const int row = tt % nrows, sg = tt / nrows;
       int u_slot[3], u_a[3];
       bool u_ok[3];
@@ -736,17 +878,16 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       if (u_ok[0]) uc0 = Us[u_a[0]];
       const int r8 = row & 7;
       const uint32_t rowoff = (uint32_t)(row >> 3) * 1024u + (uint32_t)r8 * 128u;
-      const int wmask = kCluster ? __ldg(&gp->write_mask) : 1;
       bool ok = true;
       // before reading the accumulator of a flush, generate the first
       // `ahead` stages of the item's next flush: their operands wait in
       // shared memory, so the MMAs resume as soon as the accumulator is free.
       // They reuse buffers that this flush's MMAs release, so they never wait
       // on the epilogue (ahead <= NS).
-      const int ahead = min(NS, TC_FLUSH_STAGES);
+      const int ahead = min(NS, FLUSH);
       int jdone = 0;  // stages of the item generated so far
-      for (int j0 = 0; j0 < d.nst && ok; j0 += TC_FLUSH_STAGES) {
-        const int j1 = min(d.nst, j0 + TC_FLUSH_STAGES);
+      for (int j0 = 0; j0 < d.nst && ok; j0 += FLUSH) {
+        const int j1 = min(d.nst, j0 + FLUSH);
         const int jend = min(d.nst, j1 + ahead);
         for (int j = jdone; j < jend && ok && generates; ++j, ++gs) {
           if ((int)(gs % (uint32_t)nteams) != team) continue;  // another team's stage
@@ -755,33 +896,58 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
           const int rs = (int)(gs % TC_NREC);
           if (!wait_warp(rec_full(rs), (gs / TC_NREC) & 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
           if (!wait_warp<kCluster>(smem_empty(s), par ^ 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
-          const SrcRec32* recs = reinterpret_cast<const SrcRec32*>(rec_smem + (size_t)rs * TC_REC);
+          const SrcRec32* recs = reinterpret_cast<const SrcRec32*>(rec_smem + (size_t)rs * REC);
           const uint32_t stage_op = op_base + (uint32_t)s * stage_bytes;
-          auto unit = [&](int i) {
+          // unit u (sources 8 u .. 8 u + 7 of the stage) of slot index i
+          auto unit = [&](int i, int u) {
             const uint32_t tile = stage_op + (uint32_t)u_slot[i] * TC_SLOT + rowoff;
-            uint4 re_h = make_uint4(0, 0, 0, 0), im_h = re_h, re_l = re_h, im_l = re_h;
-            if (u_ok[i]) {
-              float rv[8], iv[8];
-              gen_unit(recs + sg * 8, i == 0 ? uc0 : Us[u_a[i]], beam + u_a[i], Np, dx, dy, dlim,
-                       rv, iv);
-              split_pack(rv, re_h, re_l);
-              split_pack(iv, im_h, im_l);
+            if constexpr (kForm == 0) {
+              uint4 re_h = make_uint4(0, 0, 0, 0), im_h = re_h, re_l = re_h, im_l = re_h;
+              if (u_ok[i]) {
+                float rv[8], iv[8];
+                gen_unit(recs + u * 8, i == 0 ? uc0 : Us[u_a[i]], beam + u_a[i], Np, dx, dy,
+                         dlim, 1.f, rv, iv);
+                split_pack(rv, re_h, re_l);
+                split_pack(iv, im_h, im_l);
+              }
+              sts128(tile + ((uint32_t)(u ^ r8) << 4), re_h);
+              sts128(tile + ((uint32_t)((2 + u) ^ r8) << 4), im_h);
+              sts128(tile + ((uint32_t)((4 + u) ^ r8) << 4), re_l);
+              sts128(tile + ((uint32_t)((6 + u) ^ r8) << 4), im_l);
+            } else {
+              uint4 re_h = make_uint4(0, 0, 0, 0), im_h = re_h;
+              uint2 re_x = make_uint2(0, 0), im_x = re_x, re_l = re_x, im_l = re_x;
+              if (u_ok[i]) {
+                float rv[8], iv[8];
+                gen_unit(recs + u * 8, i == 0 ? uc0 : Us[u_a[i]], beam + u_a[i], Np, dx, dy,
+                         dlim, csc, rv, iv);
+                split_f16_e4m3(rv, re_h, re_x, re_l);
+                split_f16_e4m3(iv, im_h, im_x, im_l);
+              }
+              sts128(tile + ((uint32_t)(u ^ r8) << 4), re_h);
+              sts128(tile + ((uint32_t)((4 + u) ^ r8) << 4), im_h);
+              const uint32_t t8 = tile + tile8_off + (uint32_t)(u & 1) * 8u;
+              const int c8 = u >> 1;
+              sts64(t8 + ((uint32_t)(c8 ^ r8) << 4), re_x);
+              sts64(t8 + ((uint32_t)((2 + c8) ^ r8) << 4), im_x);
+              sts64(t8 + ((uint32_t)((4 + c8) ^ r8) << 4), re_l);
+              sts64(t8 + ((uint32_t)((6 + c8) ^ r8) << 4), im_l);
             }
-            sts128(tile + ((uint32_t)(sg ^ r8) << 4), re_h);
-            sts128(tile + ((uint32_t)((2 + sg) ^ r8) << 4), im_h);
-            sts128(tile + ((uint32_t)((4 + sg) ^ r8) << 4), re_l);
-            sts128(tile + ((uint32_t)((6 + sg) ^ r8) << 4), im_l);
           };
-          if (kCluster) {
-            // static unit indices keep the unit tables in registers (a CTA that
-            // generates owns at least one slot)
-            unit(0);
-            if (nfill > 1) unit(1);
-            if (nfill > 2) unit(2);
-          } else {
 #pragma unroll
-            for (int i = 0; i < 3; ++i)
-              if (i < nfill) unit(i);
+          for (int k = 0; k < UPT; ++k) {
+            const int u = sg * UPT + k;
+            if (kCluster) {
+              // static unit indices keep the unit tables in registers (a CTA
+              // that generates owns at least one slot)
+              unit(0, u);
+              if (nfill > 1) unit(1, u);
+              if (nfill > 2) unit(2, u);
+            } else {
+#pragma unroll
+              for (int i = 0; i < 3; ++i)
+                if (i < nfill) unit(i, u);
+            }
           }
           // operands of this stage written: one arrival per warp (each lane
           // fences its own writes for the tensor core and the copy engine)
@@ -797,7 +963,8 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
         jdone = jend;
         // ------------------------------------------------------- epilogue --
         // the sum of stages [j0, j1): stored into the partial for the first
-        // flush of the item, added to it (at L2, no load) for the later ones
+        // flush of the item, added to it (at L2, no load) for the later ones;
+        // the FP16 + FP8 form takes its slice scale out (exact)
         const bool first = j0 == 0;
         if (!wait_warp(acc_full, ic & 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
         tc_fence_after();
@@ -817,6 +984,10 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
               for (int c32 = 0; c32 < 4; ++c32) {
                 float v[32];
                 tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cb * 128 + c32 * 32), v);
+                if (kForm == 1) {
+#pragma unroll
+                  for (int c = 0; c < 32; ++c) v[c] *= inv_c2;
+                }
                 const int b0 = J * TC_ROWS + c32 * 32;
                 if (first) {
 #pragma unroll
@@ -829,7 +1000,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
             } else {
               // below the diagonal (a > b): partial[a][b] = V[b][a] = conj V[a][b],
               // 32 consecutive b per lane
-              const float sg = plane ? -1.f : 1.f;
+              const float sg_ = (plane ? -1.f : 1.f) * inv_c2;
 #pragma unroll 1
               for (int c32 = 0; c32 < 4; ++c32) {
                 float v[32];
@@ -837,8 +1008,8 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
                 float4* o4 = reinterpret_cast<float4*>(out + (size_t)a * Np + J * TC_ROWS + c32 * 32);
 #pragma unroll
                 for (int c = 0; c < 8; ++c) {
-                  const float4 x = make_float4(sg * v[4 * c], sg * v[4 * c + 1],
-                                               sg * v[4 * c + 2], sg * v[4 * c + 3]);
+                  const float4 x = make_float4(sg_ * v[4 * c], sg_ * v[4 * c + 1],
+                                               sg_ * v[4 * c + 2], sg_ * v[4 * c + 3]);
                   if (first) o4[c] = x;
                   else red_add4(o4 + c, x);
                 }
@@ -859,7 +1030,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       ItemInfo d;
       bool ok = true;
       for (long long it = it0; it < it_end && ok; it += istep) {
-        if (!decode_item<kCluster, kTable>(p, it, rank, d)) continue;
+        if (!decode_item<kCluster, kTable, KS>(p, it, rank, d)) continue;
         for (int j = 0; j < d.nst; ++j, ++gs) {
           const int r = (int)(gs % TC_NREC);
           const uint32_t par = (gs / TC_NREC) & 1;
@@ -867,10 +1038,9 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
           if (!wait1(rec_empty(r), par ^ 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
           // fault injection: stage 0 never fills, so its consumers time out
           if (p.stall && gs == 0) continue;
-          mbar_expect_tx(rec_full(r), TC_REC);
-          tma_load_2d(rec_base + (uint32_t)r * TC_REC, &rec_map, rec_full(r), 0,
-                      SIM_I(d, rec_row0) + d.tl * SIM_I(d, rec_stride) + d.s0 +
-                          j * TC_KS);
+          mbar_expect_tx(rec_full(r), REC);
+          tma_load_2d(rec_base + (uint32_t)r * REC, &rec_map, rec_full(r), 0,
+                      SIM_I(d, rec_row0) + d.tl * SIM_I(d, rec_stride) + d.s0 + j * KS);
         }
       }
       // let the copies still in flight land before the CTA can exit
@@ -886,14 +1056,15 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       bool ok = true;
       const uint16_t cmask = kCluster ? (uint16_t)__ldg(&mine->commit_mask) : (uint16_t)1;
       for (long long it = it0; it < it_end && ok; it += istep) {
-        if (!decode_item<kCluster, kTable>(p, it, rank, d)) continue;
+        if (!decode_item<kCluster, kTable, KS>(p, it, rank, d)) continue;
         const TcGroup* gp = SIM_P(d, groups) + d.g;
         const int nm = __ldg(&gp->n_mma);
-        const uint32_t idp = idesc_bf16(nm, false), idn = idesc_bf16(nm, true);
+        const uint32_t abt = kForm == 0 ? 1u : 0u;  // BF16, or FP16 / E4M3
+        const uint32_t idp = idesc_mma(nm, false, abt), idn = idesc_mma(nm, true, abt);
         const uint32_t a0 = desc_lo(op_base + (uint32_t)__ldg(&gp->sa) * TC_SLOT);
         const uint32_t b0 = desc_lo(op_base);
-        for (int j0 = 0; j0 < d.nst && ok; j0 += TC_FLUSH_STAGES) {
-          const int j1 = min(d.nst, j0 + TC_FLUSH_STAGES);
+        for (int j0 = 0; j0 < d.nst && ok; j0 += FLUSH) {
+          const int j1 = min(d.nst, j0 + FLUSH);
           // the generators have read the accumulator of the last flush
           if (!wait1(acc_empty, (ic & 1) ^ 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
           tc_fence_after();
@@ -906,7 +1077,13 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
             if (recv_bytes) mbar_expect_tx(smem_full(s), recv_bytes);
             tc_fence_after();
             const uint32_t so = ((uint32_t)s * stage_bytes) >> 4;
-            issue_group(tmem, a0 + so, b0 + so, idp, idn, j == j0);
+            if constexpr (kForm == 0) {
+              issue_group(tmem, a0 + so, b0 + so, idp, idn, j == j0);
+            } else {
+              const uint32_t o8 = tile8_off >> 4;
+              issue_group_f16f8(tmem, a0 + so, b0 + so, a0 + so + o8, b0 + so + o8, idp, idn,
+                                j == j0);
+            }
             // the stage's slots may be refilled -- here and, in cluster mode,
             // by the CTAs that wrote them -- once these MMAs have read them
             if (kCluster && cmask != (uint16_t)(1u << rank)) mma_commit_multicast(smem_empty(s), cmask);
@@ -929,7 +1106,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
     ItemInfo d;
     bool ok = true;
     for (long long it = it0; it < it_end && ok; it += istep) {
-      if (!decode_item<kCluster, kTable>(p, it, rank, d)) continue;
+      if (!decode_item<kCluster, kTable, KS>(p, it, rank, d)) continue;
       for (int j = 0; j < d.nst; ++j, ++gs) {
         const int s = (int)(gs % NS);
         const uint32_t par = (gs / NS) & 1;
@@ -941,7 +1118,10 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
           for (int q = 0; q < nd; ++q) {
             const uint32_t rr = (uint32_t)__ldg(&mine->dst_rank[k][q]);
             const uint32_t dst = stage_op + (uint32_t)__ldg(&mine->dst_slot[k][q]) * TC_SLOT;
-            bulk_push(map_to_rank(dst, rr), src, TC_SLOT, map_to_rank(smem_full(s), rr));
+#pragma unroll
+            for (int x = 0; x < TILES; ++x)
+              bulk_push(map_to_rank(dst + x * tile8_off, rr), src + x * tile8_off, TC_SLOT,
+                        map_to_rank(smem_full(s), rr));
           }
         }
       }
@@ -1088,7 +1268,6 @@ void plan_cluster(std::vector<TcGroup>& gs, int nant) {
           for (int q = 0; q < gs[o].ndst[k]; ++q)
             if (gs[o].dst_rank[k][q] == x) ++recv;
     gs[x].recv_slots = recv;
-    gs[x].full_count = (gs[x].nown > 0 ? TC_TEAM_WARPS : 0) + (recv > 0 ? 1 : 0);
     (void)writers;
     gs[x].commit_mask = commit;
     gs[x].empty_count = 1 + targets;
@@ -1144,10 +1323,16 @@ size_t tc_sim_table_bytes(int nsims) { return sizeof(TcSim) * (size_t)std::max(n
 cudaError_t tc_configure() {
   static bool done = false;
   if (done) return cudaSuccess;
-  for (const void* k : {reinterpret_cast<const void*>(tc_vis_kernel<false, false>),
-                        reinterpret_cast<const void*>(tc_vis_kernel<false, true>),
-                        reinterpret_cast<const void*>(tc_vis_kernel<true, false>),
-                        reinterpret_cast<const void*>(tc_vis_kernel<true, true>)}) {
+  for (const void* k : {reinterpret_cast<const void*>(tc_vis_kernel<false, false, 0>),
+                        reinterpret_cast<const void*>(tc_vis_kernel<false, true, 0>),
+                        reinterpret_cast<const void*>(tc_vis_kernel<true, false, 0>),
+                        reinterpret_cast<const void*>(tc_vis_kernel<true, true, 0>),
+                        reinterpret_cast<const void*>(tc_vis_kernel<false, false, 1>),
+                        reinterpret_cast<const void*>(tc_vis_kernel<false, true, 1>),
+                        reinterpret_cast<const void*>(tc_vis_kernel<true, false, 1>),
+                        reinterpret_cast<const void*>(tc_vis_kernel<true, true, 1>),
+                        reinterpret_cast<const void*>(tc_vis_kernel<true, false, 1, true>),
+                        reinterpret_cast<const void*>(tc_vis_kernel<true, true, 1, true>)}) {
     const cudaError_t e =
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_LIMIT);
     if (e != cudaSuccess) return e;
@@ -1156,18 +1341,22 @@ cudaError_t tc_configure() {
   return cudaSuccess;
 }
 
-cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, long long rec_rows,
-                            void* d_table, void* h_table, int* err, int num_sms,
-                            cudaStream_t st, unsigned long long wait_ns, int stall,
-                            TcShare* share) {
-  if (share) share->launched = 0;
-  if (nsims <= 0 || rec_rows <= 0) return cudaSuccess;
+namespace {
+
+// The launches of one fused-kernel call in form kForm (see launch_tc_batch);
+// kTeam16: cluster launches use one team of 16 generator warps per stage.
+template <int kForm, bool kTeam16>
+cudaError_t launch_form(const TcSimDesc* sims, int nsims, const void* rec, long long rec_rows,
+                        void* d_table, void* h_table, int* err, int num_sms, cudaStream_t st,
+                        unsigned long long wait_ns, int stall, TcShare* share) {
+  constexpr int KS = TcForm<kForm>::KS;
+  constexpr int TILES = TcForm<kForm>::TILES;
   auto encode = encode_fn();
   if (!encode) return cudaErrorNotSupported;
   CUtensorMap map;
   const cuuint64_t gdim[2] = {8, (cuuint64_t)rec_rows};
   const cuuint64_t gstride[1] = {sizeof(SrcRec32)};
-  const cuuint32_t box[2] = {8, TC_KS};
+  const cuuint32_t box[2] = {8, (cuuint32_t)KS};
   const cuuint32_t estride[2] = {1, 1};
   CUresult r = encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(rec), gdim,
                       gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -1192,6 +1381,7 @@ cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, l
     t.U = static_cast<const Ucoef32*>(L.U);
     t.beamT = L.beamT;
     t.umax = L.umax;
+    t.sbound = L.sbound;
     t.partial = L.partial;
     t.groups = static_cast<const TcGroup*>(L.groups);
     t.item0 = items;
@@ -1227,17 +1417,18 @@ cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, l
   p.wait_ns = wait_ns ? wait_ns : TC_WAIT_NS;
   p.stall = stall;
   p.team_warps = team_warps;
-  const int per_stage = p.max_slots * TC_SLOT;
-  const int fixed = 1024 /*alignment*/ + TC_NREC * TC_REC + 512 /*barriers, holder*/;
+  const int per_stage = TILES * p.max_slots * TC_SLOT;
+  const int fixed = 1024 /*alignment*/ + TC_NREC * KS * 32 + 512 /*barriers, holder*/;
   p.nstages = std::min(TC_MAX_STAGES, (TC_SMEM_LIMIT - fixed) / per_stage);
+  if (sims[0].tune.stages > 0) p.nstages = std::min(p.nstages, sims[0].tune.stages);
   if (p.nstages < 2) return cudaErrorInvalidConfiguration;
   const int smem = fixed + p.nstages * per_stage;
   e = tc_configure();
   if (e != cudaSuccess) return e;
   if (!cluster) {
     const long long grid = std::min<long long>(num_sms, items);
-    if (table) tc_vis_kernel<false, true><<<(int)grid, TC_THREADS, smem, st>>>(map, p);
-    else tc_vis_kernel<false, false><<<(int)grid, TC_THREADS, smem, st>>>(map, p);
+    if (table) tc_vis_kernel<false, true, kForm><<<(int)grid, TC_THREADS, smem, st>>>(map, p);
+    else tc_vis_kernel<false, false, kForm><<<(int)grid, TC_THREADS, smem, st>>>(map, p);
     return cudaGetLastError();
   }
   // cluster mode: one CTA per group, items are (slice, chunk)
@@ -1259,8 +1450,10 @@ cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, l
   static int cached_n[2][TC_MAX_CLUSTER + 1][TC_MAX_STAGES + 1] = {};
   int& nclusters = cached_n[table][C][p.nstages];
   if (nclusters == 0) {
-    e = table ? cudaOccupancyMaxActiveClusters(&nclusters, tc_vis_kernel<true, true>, &cfg)
-              : cudaOccupancyMaxActiveClusters(&nclusters, tc_vis_kernel<true, false>, &cfg);
+    e = table ? cudaOccupancyMaxActiveClusters(&nclusters, tc_vis_kernel<true, true, kForm, kTeam16>,
+                                               &cfg)
+              : cudaOccupancyMaxActiveClusters(&nclusters,
+                                               tc_vis_kernel<true, false, kForm, kTeam16>, &cfg);
     if (e != cudaSuccess) return e;
   }
   if (nclusters < 1) return cudaErrorInvalidConfiguration;
@@ -1285,12 +1478,14 @@ cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, l
     p.split = share->d_split;
     p.split_side = 0;
     cfg.stream = share->hi;
-    if ((e = cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, false>, map, p)) != cudaSuccess) return e;
+    if ((e = cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, false, kForm, kTeam16>, map, p)) !=
+        cudaSuccess)
+      return e;
     TcParams q = p;
     q.total_items = items * C;
     q.split_side = 1;
     tc_hold_kernel<<<1, 32, 0, share->lo>>>(100000ull);
-    tc_vis_kernel<false, false><<<leftover, TC_THREADS, smem, share->lo>>>(map, q);
+    tc_vis_kernel<false, false, kForm><<<leftover, TC_THREADS, smem, share->lo>>>(map, q);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = cudaEventRecord(share->join_hi, share->hi)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(share->join_lo, share->lo)) != cudaSuccess) return e;
@@ -1299,11 +1494,36 @@ cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, l
     share->launched = 4;
     return cudaSuccess;
   }
-  e = table ? cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, true>, map, p)
-            : cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, false>, map, p);
+  e = table ? cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, true, kForm, kTeam16>, map, p)
+            : cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, false, kForm, kTeam16>, map, p);
   if (e != cudaSuccess) return e;
   if (share) share->launched = 1;
   return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, long long rec_rows,
+                            void* d_table, void* h_table, int* err, int num_sms,
+                            cudaStream_t st, unsigned long long wait_ns, int stall,
+                            TcShare* share) {
+  if (share) share->launched = 0;
+  if (nsims <= 0 || rec_rows <= 0) return cudaSuccess;
+  // one form per launch
+  for (int i = 1; i < nsims; ++i)
+    if (sims[i].form != sims[0].form) return cudaErrorInvalidValue;
+  if (sims[0].form == 1) {
+    for (int i = 0; i < nsims; ++i)
+      if (!sims[i].sbound) return cudaErrorInvalidValue;
+    if (sims[0].tune.team_warps == 16)
+      return launch_form<1, true>(sims, nsims, rec, rec_rows, d_table, h_table, err, num_sms, st,
+                                  wait_ns, stall, share);
+    return launch_form<1, false>(sims, nsims, rec, rec_rows, d_table, h_table, err, num_sms, st,
+                                 wait_ns, stall, share);
+  }
+  if (sims[0].form != 0) return cudaErrorInvalidValue;
+  return launch_form<0, false>(sims, nsims, rec, rec_rows, d_table, h_table, err, num_sms, st,
+                               wait_ns, stall, share);
 }
 
 size_t tc_partial_floats(int Np, int nsrc, int nslices, int chunk) {

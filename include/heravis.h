@@ -57,8 +57,12 @@ typedef enum {
   HV_METHOD_PLAIN = 1,    /* the reference's method: phasors to HBM, then an
                              FP32 (precision 1) / FP64 (precision 2) SIMT
                              Hermitian product                                 */
-  HV_METHOD_TC_BF16 = 2   /* fused: phasors generated in shared memory, split
+  HV_METHOD_TC_BF16 = 2,  /* fused: phasors generated in shared memory, split
                              BF16 tcgen05 products, FP32 accumulation in TMEM  */
+  HV_METHOD_TC_FP16 = 3   /* fused, FP16 hi products and E4M3 (FP8) cross
+                             terms of a per-(time, frequency) power-of-two
+                             scaled split, FP32 accumulation in TMEM: about
+                             2/3 of the tensor-core time of TC_BF16          */
 } hv_method;
 
 typedef struct hv_context hv_context;
@@ -126,6 +130,22 @@ int hv_profile_read(hv_context* ctx, double* ms, uint64_t* launches);
  * HV_ERR_TIMEOUT with the context still usable.  No counterpart in the
  * reference (it has no device-side waits, hera_gpu/vis.py:144-250). */
 int hv_set_wait_limit(hv_context* ctx, uint64_t wait_ns, int stall);
+
+/* Launch shape of the fused kernel for this context's later calls (the
+ * batched form takes the same knobs from its autotuner).  No counterpart in
+ * the reference, whose launch geometry is a fixed formula (vis.py:176-180).
+ * value 0 restores the default of `param`:
+ *   HV_TUNE_TEAM_WARPS  8 (default): two teams of 8 generator warps take
+ *                       alternate stages; 16: one team per stage
+ *                       (HV_METHOD_TC_FP16 on 129-1024 antennas only; other
+ *                       calls ignore it)
+ *   HV_TUNE_STAGES      cap on the operand stages held in shared memory,
+ *                       2..8 (default: as many as fit) */
+enum {
+  HV_TUNE_TEAM_WARPS = 1,
+  HV_TUNE_STAGES = 2
+};
+int hv_set_tuning(hv_context* ctx, int param, int value);
 
 /* ---- batched form -------------------------------------------------------
  * Many independent simulations (precision 1, fused tensor-core form) planned

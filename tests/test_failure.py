@@ -26,18 +26,19 @@ def config(nant, nsrc, ntimes=2, nfreq=2, seed=5):
             cfg["crd_eq"].astype(np.float32), cfg["I_sky"].astype(np.float32), bm)
 
 
+@pytest.mark.parametrize("method", ["tc", "tc_fp16"])
 @pytest.mark.parametrize("nant", [40, 300])  # one CTA per item; a cluster of three
-def test_injected_stall_times_out_and_context_recovers(nant):
+def test_injected_stall_times_out_and_context_recovers(nant, method):
     args = config(nant, 3000)
     ctx = _native.Context(0)
-    ref = vis_gpu_multifreq(*args, precision=1, method="tc", context=ctx)
+    ref = vis_gpu_multifreq(*args, precision=1, method=method, context=ctx)
     ctx.set_wait_limit(0.05, stall=True)
     t0 = time.perf_counter()
     with pytest.raises(_native.HeraVisTimeout):
-        vis_gpu_multifreq(*args, precision=1, method="tc", context=ctx)
+        vis_gpu_multifreq(*args, precision=1, method=method, context=ctx)
     assert time.perf_counter() - t0 < 30.0
     ctx.set_wait_limit(0.0, stall=False)
-    again = vis_gpu_multifreq(*args, precision=1, method="tc", context=ctx)
+    again = vis_gpu_multifreq(*args, precision=1, method=method, context=ctx)
     np.testing.assert_array_equal(again, ref)
 
 

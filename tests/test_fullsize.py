@@ -39,11 +39,12 @@ def full():
     args = (cfg["antpos"].astype(np.float32), cfg["freqs"], cfg["eq2tops"].astype(np.float32),
             cfg["crd_eq"].astype(np.float32), cfg["I_sky"].astype(np.float32), bm)
     V = vis_gpu_multifreq(*args, precision=1, method="tc")
-    return args, V
+    V16 = vis_gpu_multifreq(*args, precision=1, method="tc_fp16")
+    return args, V, V16
 
 
 def test_fullsize_hermitian(full):
-    _, V = full
+    _, V, _ = full
     assert V.shape == (64, 2, 350, 350) and V.dtype == np.complex64
     np.testing.assert_array_equal(V, np.conj(np.swapaxes(V, -1, -2)))
     d = np.diagonal(V, axis1=-2, axis2=-1)
@@ -52,16 +53,17 @@ def test_fullsize_hermitian(full):
 
 @pytest.mark.parametrize("t,f", [(0, 0), (1, 63)])
 def test_fullsize_autocorrelations(full, t, f):
-    (antpos, freqs, e2t, crd, I, bm), V = full
+    (antpos, freqs, e2t, crd, I, bm), V, V16 = full
     top = as_seen(e2t[t]) @ as_seen(crd)
     up = top[2] > 0
     tx, ty = top[0, up], top[1, up]
     Iu = as_seen(I)[up]
     beams = as_seen(bm[f])
     ref = np.array([np.dot(bilinear_beam(beams[a], tx, ty) ** 2, Iu) for a in range(350)])
-    got = np.diagonal(V[f, t]).real.astype(np.float64)
-    err = np.abs(got - ref) / ref
-    assert err.max() <= 1e-4, err.max()
+    for out in (V, V16):
+        got = np.diagonal(out[f, t]).real.astype(np.float64)
+        err = np.abs(got - ref) / ref
+        assert err.max() <= 1e-4, err.max()
 
 
 def oracle_slice(args, t, f, block=131072):
@@ -78,13 +80,15 @@ def oracle_slice(args, t, f, block=131072):
 
 @pytest.mark.parametrize("t,f", [(0, 0), (1, 63)])
 def test_fullsize_slice_against_oracle(full, t, f):
-    args, V = full
-    err = rel_frobenius(V[f, t], oracle_slice(args, t, f))
-    assert err <= 1e-4, err
+    args, V, V16 = full
+    ref = oracle_slice(args, t, f)
+    for name, out in (("tc", V), ("tc_fp16", V16)):
+        err = rel_frobenius(out[f, t], ref)
+        assert err <= 1e-4, (name, err)
 
 
 def test_fullsize_linear_in_the_sources(full):
-    (antpos, freqs, e2t, crd, I, bm), V = full
+    (antpos, freqs, e2t, crd, I, bm), V, _ = full
     chans = np.arange(0, 64, 8)
     h = crd.shape[1] // 2
     part = lambda s: vis_gpu_multifreq(antpos, freqs[chans], e2t[:1], crd[:, s],
@@ -115,7 +119,7 @@ def array_scale(precision):
 
 
 @pytest.mark.parametrize("method,precision,tol", [("plain", 1, 1e-5), ("tc", 1, 1e-4),
-                                                  ("plain", 2, 1e-11)])
+                                                  ("tc_fp16", 1, 1e-4), ("plain", 2, 1e-11)])
 def test_array_scale_against_oracle(method, precision, tol):
     args, ref = array_scale(precision)
     V = vis_gpu(*args, precision=precision, method=method)

@@ -2,9 +2,10 @@
 
 Tolerances (relative Frobenius error per time slice, vs the FP64 oracle run
 on the same inputs as the GPU saw):
-    plain, precision 1 (FP32 SIMT product)       <= 1e-5
-    tc,    precision 1 (split-BF16 tensor cores) <= 1e-4
-    plain, precision 2 (FP64)                    <= 1e-11
+    plain,   precision 1 (FP32 SIMT product)                    <= 1e-5
+    tc,      precision 1 (split-BF16 tensor cores)              <= 1e-4
+    tc_fp16, precision 1 (FP16 + E4M3 split, tensor cores)      <= 1e-4
+    plain,   precision 2 (FP64)                                 <= 1e-11
 The FP64 bound is set by FP64 rounding of phases of ~1e3 cycles (the
 km-baseline fixture), where the oracle itself carries errors of 1e-12.
 """
@@ -20,9 +21,9 @@ from vis_gpu_cases import VIS_GPU_CASES, load_vis_gpu_case
 pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
-TOL = {("plain", 1): 1e-5, ("tc", 1): 1e-4, ("plain", 2): 1e-11, ("auto", 1): 1e-4,
-       ("auto", 2): 1e-11}
-METHODS = [("plain", 1), ("plain", 2), ("tc", 1)]
+TOL = {("plain", 1): 1e-5, ("tc", 1): 1e-4, ("tc_fp16", 1): 1e-4, ("plain", 2): 1e-11,
+       ("auto", 1): 1e-4, ("auto", 2): 1e-11}
+METHODS = [("plain", 1), ("plain", 2), ("tc", 1), ("tc_fp16", 1)]
 
 
 def as_seen(x, precision):
@@ -91,6 +92,10 @@ def test_kat_values(method, precision):
     # co-located antennas, every source at zenith: V = NPIX (decimal 22 in the reference)
     v = vis_gpu(antpos, 1.0, eq2tops, crd_eq, I_sky, bm, **kw)
     np.testing.assert_almost_equal(v, NPIX, 22 if precision == 2 or method == "plain" else 3)
+    if method == "tc_fp16":
+        # every source at the beam's peak, |X| = 256 exactly: the scaled
+        # split is exact, so the sum is too
+        np.testing.assert_equal(v, NPIX)
     # two sources, at zenith and at 45 deg: V ~ 2
     crd2 = np.zeros((3, 2))
     crd2[2, 0] = 1
@@ -194,3 +199,36 @@ def test_deterministic(method, precision):
     a = vis_gpu(*args, precision=precision, method=method)
     b = vis_gpu(*args, precision=precision, method=method)
     np.testing.assert_array_equal(a, b)
+
+
+def test_fp16_form_scales_each_slice():
+    # the FP16 + FP8 form scales each (time, frequency) slice by its own
+    # power of two: skies of very different brightness per channel (the beam
+    # differs by 2^40 between channels) keep the same relative accuracy
+    cfg = synth.config_array(seed=8, nant=60, nsrc=4000, ntimes=2, nfreq=3, fmin=100e6,
+                             fmax=200e6, P=31)
+    bms = synth.beams_for(cfg, dtype=np.float64)
+    bms *= np.array([1e-6, 1.0, 1e6])[:, None, None, None]
+    I = cfg["I_sky"] * 1e3
+    v = vis_gpu_multifreq(cfg["antpos"], cfg["freqs"], cfg["eq2tops"], cfg["crd_eq"], I, bms,
+                          precision=1, method="tc_fp16")
+    for f in range(3):
+        ref = oracle_same_inputs((cfg["antpos"], cfg["freqs"][f], cfg["eq2tops"], cfg["crd_eq"],
+                                  I, bms[f]), 1)
+        assert rel_frobenius(v[f], ref).max() <= 1e-4, f
+
+
+@pytest.mark.parametrize("team_warps,stages", [(16, 0), (8, 2), (16, 2)])
+def test_fp16_launch_shapes_agree(team_warps, stages):
+    # the tuning knobs change how the work is laid out on the SM, not the
+    # arithmetic: every shape gives the default's result bit for bit
+    from hera_gpu_gb300 import _native
+    cfg = synth.config_array(seed=9, nant=300, nsrc=6000, ntimes=2, nfreq=2, fmin=100e6,
+                             fmax=200e6, P=31)
+    bms = synth.beams_for(cfg, dtype=np.float32)
+    args = (cfg["antpos"], cfg["freqs"], cfg["eq2tops"], cfg["crd_eq"], cfg["I_sky"], bms)
+    ctx = _native.Context(0)
+    ref = vis_gpu_multifreq(*args, precision=1, method="tc_fp16", context=ctx)
+    ctx.set_tuning(team_warps=team_warps, stages=stages)
+    got = vis_gpu_multifreq(*args, precision=1, method="tc_fp16", context=ctx)
+    np.testing.assert_array_equal(got, ref)
