@@ -1422,6 +1422,17 @@ cudaError_t launch_form(const TcSimDesc* sims, int nsims, const void* rec, long 
   p.nstages = std::min(TC_MAX_STAGES, (TC_SMEM_LIMIT - fixed) / per_stage);
   if (sims[0].tune.stages > 0) p.nstages = std::min(p.nstages, sims[0].tune.stages);
   if (p.nstages < 2) return cudaErrorInvalidConfiguration;
+  // A team waits on a stage's barriers by phase parity, which tells apart
+  // only consecutive phases: a team may run at most one round of a stage
+  // ahead of the MMAs, which holds while the teams are no more than the
+  // stages (each team's previous stage was released before it).  Small
+  // teams of one-slot launches are widened until that holds.
+  while (TC_GEN_WARPS / p.team_warps > p.nstages && p.team_warps < TC_TEAM_WARPS)
+    p.team_warps *= 2;
+  const int cl_team = kTeam16 ? 16 : TC_TEAM_WARPS;
+  if (TC_GEN_WARPS / p.team_warps > p.nstages || TC_GEN_WARPS / cl_team > p.nstages ||
+      TC_GEN_WARPS / p.team_warps > TC_NREC)
+    return cudaErrorInvalidConfiguration;
   const int smem = fixed + p.nstages * per_stage;
   e = tc_configure();
   if (e != cudaSuccess) return e;
