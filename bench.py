@@ -65,6 +65,10 @@ def parse_args():
     ap.add_argument("--method", default="tc", choices=["tc", "tc_fp16", "plain"])
     ap.add_argument("--no-forms", action="store_true",
                     help="skip timing the other fused form on the same steps")
+    ap.add_argument("--team-warps", type=int, default=0,
+                    help="fused kernel: generator warps per stage (0 = default; 16 for tc_fp16)")
+    ap.add_argument("--stages", type=int, default=0,
+                    help="fused kernel: cap on operand stages in shared memory (0 = default)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
@@ -398,6 +402,7 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     ctx = _native.Context(local)
+    ctx.set_tuning(team_warps=args.team_warps, stages=args.stages)
     num_sms = torch.cuda.get_device_properties(local).multi_processor_count
     w = make_workload(args.nant, args.nsrc, args.nfreq, seed=rank)
     N, S, F = args.nant, args.nsrc, args.nfreq
@@ -578,6 +583,7 @@ def run_ours(args):
         for m in methods:
             for t0 in sorted({min(t, NTIMES - T_PER_STEP) for t, _ in corners}):
                 step(0, m, t0)
+                torch.cuda.synchronize(dev)   # the call ran on `stream`
                 ctx.sync()
                 for t, f in corners:
                     if t0 <= t < t0 + T_PER_STEP:

@@ -45,6 +45,9 @@ struct hv_context {
   // a fused launch of one simulation shared between its cluster kernel and a
   // one-CTA kernel on the SMs no cluster fits on (launch_tc_batch)
   hv::TcShare share{};
+  // end of a device-API call made on a caller's stream: the context's stream
+  // waits on it, so hv_sync and the error-flag read come after that work
+  cudaEvent_t joined = nullptr;
   size_t budget = 0;  // 0 = unlimited
   size_t held = 0;
   std::string err;
@@ -461,7 +464,8 @@ int hv_create(hv_context** out, int device, size_t hbm_budget_bytes) {
         cudaStreamCreateWithPriority(&ctx->share.lo, cudaStreamNonBlocking, least) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->share.fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->share.join_hi, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->share.join_lo, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&ctx->share.join_lo, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->joined, cudaEventDisableTiming) != cudaSuccess) {
       r = HV_ERR_CUDA;
       break;
     }
@@ -503,7 +507,7 @@ int hv_destroy(hv_context* ctx) {
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   if (ctx->share.hi) cudaStreamDestroy(ctx->share.hi);
   if (ctx->share.lo) cudaStreamDestroy(ctx->share.lo);
-  for (cudaEvent_t ev : {ctx->share.fork, ctx->share.join_hi, ctx->share.join_lo})
+  for (cudaEvent_t ev : {ctx->share.fork, ctx->share.join_hi, ctx->share.join_lo, ctx->joined})
     if (ev) cudaEventDestroy(ev);
   delete ctx;
   return HV_OK;
@@ -532,8 +536,19 @@ int hv_vis_multifreq_device(hv_context* ctx, int precision, int method, const vo
     return fail(ctx, HV_ERR_ARG, "null array argument");
   HV_CK(cudaSetDevice(ctx->device));
   cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
-  return dispatch_device(ctx, precision, method, d_antpos, nant, freqs, nfreq, d_eq2tops,
-                         ntimes, d_crd_eq, d_I_sky, nsrc, d_bm_cubes, beam_px, d_vis_out, st);
+  r = dispatch_device(ctx, precision, method, d_antpos, nant, freqs, nfreq, d_eq2tops, ntimes,
+                      d_crd_eq, d_I_sky, nsrc, d_bm_cubes, beam_px, d_vis_out, st);
+  if (r != HV_OK || st == ctx->stream) return r;
+  // the context's stream follows the call's work (not while the caller's
+  // stream is being captured: that would pull the context's stream into the
+  // capture), so that hv_sync waits for it and reads its error flag after it
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  HV_CK(cudaStreamIsCapturing(st, &cap));
+  if (cap == cudaStreamCaptureStatusNone) {
+    HV_CK(cudaEventRecord(ctx->joined, st));
+    HV_CK(cudaStreamWaitEvent(ctx->stream, ctx->joined, 0));
+  }
+  return HV_OK;
 }
 
 int hv_vis_multifreq(hv_context* ctx, int precision, int method, const void* antpos, int nant,

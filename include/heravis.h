@@ -102,7 +102,10 @@ int hv_vis_multifreq(hv_context* ctx, int precision, int method,
 /* As hv_vis_multifreq with every array already in device memory (freqs
  * stays a host array).  Work is ordered on `stream` (a cudaStream_t; NULL =
  * the context's stream) and the call returns without synchronising; call
- * hv_sync() before reading `d_vis_out` on another stream or the host. */
+ * hv_sync() before reading `d_vis_out` on another stream or the host (the
+ * context's stream is made to wait for the call's work on `stream`, unless
+ * `stream` is being captured into a graph; then synchronise `stream`
+ * itself). */
 int hv_vis_multifreq_device(hv_context* ctx, int precision, int method,
                             const void* d_antpos, int nant,
                             const double* freqs, int nfreq,

@@ -232,3 +232,33 @@ def test_fp16_launch_shapes_agree(team_warps, stages):
     ctx.set_tuning(team_warps=team_warps, stages=stages)
     got = vis_gpu_multifreq(*args, precision=1, method="tc_fp16", context=ctx)
     np.testing.assert_array_equal(got, ref)
+
+
+def test_sync_covers_a_call_on_the_callers_stream():
+    # hv_vis_multifreq_device on a stream of the caller's, then hv_sync on
+    # the context: the output is complete when hv_sync returns, without the
+    # caller synchronising its own stream (the output starts as NaN, and the
+    # call is long enough to still be running otherwise)
+    import torch
+    from hera_gpu_gb300 import _native
+    cfg = synth.config_array(seed=4, nant=300, nsrc=200_000, ntimes=4, nfreq=8, fmin=100e6,
+                             fmax=200e6, P=31)
+    bms = synth.beams_for(cfg, dtype=np.float32)
+    host = {k: np.ascontiguousarray(cfg[k], dtype=np.float32)
+            for k in ("antpos", "eq2tops", "crd_eq", "I_sky")}
+    dev = torch.device("cuda", 0)
+    d = {k: torch.from_numpy(v).to(dev) for k, v in host.items()}
+    d_bm = torch.from_numpy(bms).to(dev)
+    ctx = _native.Context(0)
+    ref = vis_gpu_multifreq(host["antpos"], cfg["freqs"], host["eq2tops"], host["crd_eq"],
+                            host["I_sky"], bms, precision=1, method="tc", context=ctx)
+    out = torch.full(ref.shape, float("nan"), dtype=torch.complex64, device=dev)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.synchronize(dev)
+    ctx.vis_multifreq_device(1, "tc", d["antpos"].data_ptr(), 300, cfg["freqs"],
+                             d["eq2tops"].data_ptr(), 4, d["crd_eq"].data_ptr(),
+                             d["I_sky"].data_ptr(), 200_000, d_bm.data_ptr(), 31, out.data_ptr(),
+                             stream.cuda_stream)
+    ctx.sync()
+    got = out.cpu().numpy()   # a copy on the default stream, not ordered after `stream`
+    np.testing.assert_array_equal(got, ref)
