@@ -65,8 +65,6 @@ def parse_args():
     ap.add_argument("--method", default="tc", choices=["tc", "tc_fp16", "plain"])
     ap.add_argument("--no-forms", action="store_true",
                     help="skip timing the other fused form on the same steps")
-    ap.add_argument("--team-warps", type=int, default=0,
-                    help="fused kernel: generator warps per stage (0 = default; 16 for tc_fp16)")
     ap.add_argument("--stages", type=int, default=0,
                     help="fused kernel: cap on operand stages in shared memory (0 = default)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
@@ -402,7 +400,7 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     ctx = _native.Context(local)
-    ctx.set_tuning(team_warps=args.team_warps, stages=args.stages)
+    ctx.set_tuning(stages=args.stages)
     num_sms = torch.cuda.get_device_properties(local).multi_processor_count
     w = make_workload(args.nant, args.nsrc, args.nfreq, seed=rank)
     N, S, F = args.nant, args.nsrc, args.nfreq

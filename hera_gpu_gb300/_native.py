@@ -36,7 +36,6 @@ class HvSim(ctypes.Structure):
 HV_BATCH_GRAPH = 1
 HV_BATCH_AUTOTUNE = 2
 
-HV_TUNE_TEAM_WARPS = 1
 HV_TUNE_STAGES = 2
 
 # Every function of the ABI: name -> (restype, argtypes)
@@ -227,10 +226,9 @@ class Context:
         injection for tests of failure detection)."""
         self.check(self.lib.hv_set_wait_limit(self.h, int(wait_s * 1e9), 1 if stall else 0))
 
-    def set_tuning(self, team_warps: int = 0, stages: int = 0):
+    def set_tuning(self, stages: int = 0):
         """Launch shape of the fused kernel for later calls (hv_set_tuning;
-        0 = the default of each)."""
-        self.check(self.lib.hv_set_tuning(self.h, HV_TUNE_TEAM_WARPS, int(team_warps)))
+        0 = the default)."""
         self.check(self.lib.hv_set_tuning(self.h, HV_TUNE_STAGES, int(stages)))
 
     def median_filter(self, images, out, k0, k1):

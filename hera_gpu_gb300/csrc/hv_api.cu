@@ -607,11 +607,6 @@ int hv_set_profiling(hv_context* ctx, int enable) {
 int hv_set_tuning(hv_context* ctx, int param, int value) {
   if (!ctx) return HV_ERR_ARG;
   switch (param) {
-    case HV_TUNE_TEAM_WARPS:
-      if (value != 0 && value != 8 && value != 16)
-        return fail(ctx, HV_ERR_ARG, "team warps must be 0, 8 or 16 (got %d)", value);
-      ctx->tune.team_warps = value;
-      return HV_OK;
     case HV_TUNE_STAGES:
       if (value != 0 && (value < 2 || value > 8))
         return fail(ctx, HV_ERR_ARG, "stages must be 0 or in [2, 8] (got %d)", value);

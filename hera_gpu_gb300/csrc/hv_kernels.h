@@ -97,8 +97,7 @@ cudaError_t launch_reduce(const R* partial, size_t slice_stride, const int* coun
 // --- hv_tc.cu --------------------------------------------------------------
 // Launch shape of the fused kernel; 0 everywhere = the defaults.
 struct TcTune {
-  int team_warps;  // 16: one generator team of 16 warps per stage (FP16 + FP8 cluster launches)
-  int stages;      // cap on the operand stages in shared memory (>= 2)
+  int stages;  // cap on the operand stages in shared memory (>= the generator teams)
 };
 // One simulation of a fused-kernel launch (device pointers).
 struct TcSimDesc {

@@ -99,12 +99,31 @@ constexpr int TC_REC_MAX = TC_KS_MAX * 32;  // bytes of source records per stage
 // producer runs further ahead and a generator warp finds its next records
 // loaded even while slower warps still hold earlier stages.
 constexpr int TC_NREC = 8;
-constexpr int TC_GEN_WARPS = 16;
-constexpr int TC_GEN_THREADS = TC_GEN_WARPS * 32;
-// Generator warps per stage: 8 (two teams on alternate stages); one-slot
-// launches of up to 64 (32) antennas use teams of 4 (2) warps, enough for
-// their rows, so that 4 (8) stages are generated at once.
-constexpr int TC_TEAM_WARPS = 8;
+// Warp layout of each form.  The SM's four schedulers each hold a quarter
+// of the block's warps, and a scheduler's 16K-register file is shared by
+// its warps.
+//  * Split BF16: 12 generator warps + 3 service warps (15; at most 4 a
+//    scheduler), so a thread may hold 128 registers; teams of 4 warps, one
+//    thread per antenna row generating all 16 sources of it per stage, three
+//    teams taking the stages in turn.  Measured against 16 generator warps
+//    at 96 registers (teams of 8): 7% faster at 350 antennas x 1M sources.
+//  * FP16 + FP8: 16 generator warps + 3 service (19; 96 registers), one team
+//    of 16 per 32-source stage (four thread groups along the stage, one
+//    unit of 8 sources each).  Only three of its 64 KB stages fit beside the
+//    records, so a stage must be generated by every generator at once: with
+//    12 warps in three teams it ran 10% slower.
+// One-slot launches of up to 64 (32) antennas use teams of half (a
+// quarter) the full team, enough for their rows.
+template <int kForm> struct TcLayout;
+template <> struct TcLayout<0> {
+  static constexpr int GEN_WARPS = 12, TEAM = 4, NSG = 1;
+};
+template <> struct TcLayout<1> {
+  static constexpr int GEN_WARPS = 16, TEAM = 16, NSG = 4;
+};
+template <int kForm> constexpr int tc_threads() { return TcLayout<kForm>::GEN_WARPS * 32 + 96; }
+static_assert(((tc_threads<0>() / 32 + 3) / 4) * 32 * 128 <= 16384,
+              "split BF16: at most 4 warps a scheduler at 128 registers");
 constexpr int TC_MAX_STAGES = 8;
 // Sources accumulated in TMEM before the sum is added to the item's split-K
 // partial in global memory (FP32, round to nearest) and the accumulator
@@ -119,10 +138,6 @@ constexpr int TC_MAX_STAGES = 8;
 #define TC_FLUSH_SOURCES 2048
 #endif
 static_assert(TC_FLUSH_SOURCES % TC_KS_MAX == 0, "flush interval: whole stages of every form");
-constexpr int TC_PRODUCER_WARP = TC_GEN_WARPS;
-constexpr int TC_MMA_WARP = TC_GEN_WARPS + 1;
-constexpr int TC_PUSH_WARP = TC_GEN_WARPS + 2;  // cluster mode: pushes tiles to peer CTAs
-constexpr int TC_THREADS = TC_GEN_THREADS + 96;
 constexpr int TC_TMEM_COLS = 512;
 constexpr int TC_SMEM_LIMIT = 227 * 1024;
 constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // default limit of one wait: 2 s
@@ -724,22 +739,28 @@ __device__ __forceinline__ bool decode_item(const TcParams& p, long long it, int
 
 // 19 warps on 4 schedulers: the busiest scheduler holds 5 warps, and its
 // 16K-register file caps a thread at 96 registers (launch bounds give that).
-// kTeam16 (FP16 + FP8 form): one team of 16 generator warps per stage in
-// cluster mode, instead of two teams of 8 taking alternate stages.
-template <bool kCluster, bool kTable, int kForm, bool kTeam16 = false>
-__global__ void __launch_bounds__(TC_THREADS, 1)
+template <bool kCluster, bool kTable, int kForm>
+__global__ void __launch_bounds__(tc_threads<kForm>(), 1)
 tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant__ TcParams p) {
+  // warp roles: generators, then the TMA producer, the MMA issuer and the
+  // cluster-mode pusher of tiles to peer CTAs
+  constexpr int TC_GEN_WARPS = TcLayout<kForm>::GEN_WARPS;
+  constexpr int TC_GEN_THREADS = TC_GEN_WARPS * 32;
+  constexpr int TC_PRODUCER_WARP = TC_GEN_WARPS;
+  constexpr int TC_MMA_WARP = TC_GEN_WARPS + 1;
+  constexpr int TC_PUSH_WARP = TC_GEN_WARPS + 2;
   constexpr int KS = TcForm<kForm>::KS;         // sources per stage
   constexpr int TILES = TcForm<kForm>::TILES;   // tiles per slot per stage
   constexpr int REC = KS * 32;                  // record bytes per stage
   constexpr int FLUSH = TC_FLUSH_SOURCES / KS;  // stages per accumulator flush
   // generator warps per stage in cluster mode (compile-time there; launches
   // without clusters take theirs from the parameters)
-  constexpr int CL_TEAM = kTeam16 ? 16 : TC_TEAM_WARPS;
-  static_assert(!kTeam16 || (kForm == 1 && kCluster), "16-warp teams: FP16 + FP8 cluster launches");
+  constexpr int CL_TEAM = TcLayout<kForm>::TEAM;
   extern __shared__ uint8_t smem_raw[];
-  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
-                                             ~uintptr_t(1023));
+  // 1024-byte aligned base, formed by adding to the shared array (not by
+  // integer casts) so that every pointer derived from it stays a shared
+  // pointer and its loads are shared-memory loads, not generic ones
+  uint8_t* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   const int NS = p.nstages;
   const uint32_t op_base = smem_u32(smem);
   // a stage: the FP16 / split-BF16 tiles of every slot side by side, then
@@ -855,12 +876,12 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       // units of 8 sources [sg * upt, sg * upt + upt) of its team's stages,
       // in each slot it fills
       // a team covers its rows (128, or fewer for the small teams of
-      // one-slot launches) with 2 thread groups along the stage, or 4 for a
-      // team of 16
-      constexpr int NSG = kTeam16 ? 4 : 2;
+      // one-slot launches) with NSG thread groups along the stage
+      constexpr int NSG = TcLayout<kForm>::NSG;
       constexpr int UPT = (KS / 8) / NSG;  // units per thread per stage
-      const int tt = tid & (team_warps * 32 - 1);
-      const int nrows = kCluster ? TC_ROWS : team_warps * 16;
+      static_assert(UPT >= 1 && UPT * NSG * 8 == KS, "a stage's units split evenly");
+      const int tt = tid % (team_warps * 32);
+      const int nrows = kCluster ? TC_ROWS : team_warps * 32 / NSG;
       const int row = tt % nrows, sg = tt / nrows;
       int u_slot[3], u_a[3];
       bool u_ok[3];
@@ -934,7 +955,9 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
               sts64(t8 + ((uint32_t)((6 + c8) ^ r8) << 4), im_l);
             }
           };
-#pragma unroll
+          // one copy of the unit code (a second unrolled copy costs more in
+          // instruction-cache misses than its static indices save)
+#pragma unroll 1
           for (int k = 0; k < UPT; ++k) {
             const int u = sg * UPT + k;
             if (kCluster) {
@@ -968,10 +991,12 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
         const bool first = j0 == 0;
         if (!wait_warp(acc_full, ic & 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
         tc_fence_after();
-        {
-          // lane quadrant q, 128-column block cb of TMEM: pair cb & 1, plane
-          // cb >> 1 (Re, Im)
-          const int q = warp & 3, cb = warp >> 2;
+        // a warp reads its lane quadrant q of TMEM; its 128-column blocks cb
+        // (pair cb & 1, plane cb >> 1: Re, Im) are every (generator warps /
+        // 4)-th from warp / 4
+#pragma unroll 1
+        for (int cb = warp >> 2; cb < 4; cb += TC_GEN_WARPS / 4) {
+          const int q = warp & 3;
           const int pr = cb & 1, plane = cb >> 1;
           if (pr < g_npairs) {
             const int I = __ldg(&gp->pI[pr]), J = __ldg(&gp->pJ[pr]);
@@ -1293,7 +1318,15 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 
 int tc_num_groups(int nant) { return (int)make_groups(nant).size(); }
 
-int tc_team_warps(int nant) { return nant <= 32 ? 2 : nant <= 64 ? 4 : TC_TEAM_WARPS; }
+namespace {
+template <int kForm>
+int team_warps_for(int nant) {
+  constexpr int T = TcLayout<kForm>::TEAM;
+  return nant <= 32 ? T / 4 : nant <= 64 ? T / 2 : T;
+}
+}  // namespace
+
+int tc_team_warps(int nant) { return team_warps_for<0>(nant); }
 
 size_t tc_group_table_bytes(int nant) { return sizeof(TcGroup) * make_groups(nant).size(); }
 
@@ -1330,9 +1363,7 @@ cudaError_t tc_configure() {
                         reinterpret_cast<const void*>(tc_vis_kernel<false, false, 1>),
                         reinterpret_cast<const void*>(tc_vis_kernel<false, true, 1>),
                         reinterpret_cast<const void*>(tc_vis_kernel<true, false, 1>),
-                        reinterpret_cast<const void*>(tc_vis_kernel<true, true, 1>),
-                        reinterpret_cast<const void*>(tc_vis_kernel<true, false, 1, true>),
-                        reinterpret_cast<const void*>(tc_vis_kernel<true, true, 1, true>)}) {
+                        reinterpret_cast<const void*>(tc_vis_kernel<true, true, 1>)}) {
     const cudaError_t e =
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_LIMIT);
     if (e != cudaSuccess) return e;
@@ -1343,14 +1374,16 @@ cudaError_t tc_configure() {
 
 namespace {
 
-// The launches of one fused-kernel call in form kForm (see launch_tc_batch);
-// kTeam16: cluster launches use one team of 16 generator warps per stage.
-template <int kForm, bool kTeam16>
+// The launches of one fused-kernel call in form kForm (see launch_tc_batch).
+template <int kForm>
 cudaError_t launch_form(const TcSimDesc* sims, int nsims, const void* rec, long long rec_rows,
                         void* d_table, void* h_table, int* err, int num_sms, cudaStream_t st,
                         unsigned long long wait_ns, int stall, TcShare* share) {
   constexpr int KS = TcForm<kForm>::KS;
   constexpr int TILES = TcForm<kForm>::TILES;
+  constexpr int TC_GEN_WARPS = TcLayout<kForm>::GEN_WARPS;
+  constexpr int TC_TEAM_WARPS = TcLayout<kForm>::TEAM;
+  constexpr int TC_THREADS = tc_threads<kForm>();
   auto encode = encode_fn();
   if (!encode) return cudaErrorNotSupported;
   CUtensorMap map;
@@ -1366,11 +1399,11 @@ cudaError_t launch_form(const TcSimDesc* sims, int nsims, const void* rec, long 
 
   // cluster mode when every simulation has the same (clusterable) group layout
   bool cluster = use_cluster(sims[0].ngroups);
-  int max_slots = 1, team_warps = 2;
+  int max_slots = 1, team_warps = 1;
   for (int i = 0; i < nsims; ++i) {
     if (sims[i].ngroups != sims[0].ngroups) cluster = false;
     max_slots = std::max(max_slots, sims[i].max_slots);
-    team_warps = std::max(team_warps, tc_team_warps(sims[i].nant));
+    team_warps = std::max(team_warps, team_warps_for<kForm>(sims[i].nant));
   }
   TcSim* tab = static_cast<TcSim*>(h_table);
   long long items = 0;
@@ -1419,19 +1452,20 @@ cudaError_t launch_form(const TcSimDesc* sims, int nsims, const void* rec, long 
   p.team_warps = team_warps;
   const int per_stage = TILES * p.max_slots * TC_SLOT;
   const int fixed = 1024 /*alignment*/ + TC_NREC * KS * 32 + 512 /*barriers, holder*/;
-  p.nstages = std::min(TC_MAX_STAGES, (TC_SMEM_LIMIT - fixed) / per_stage);
+  const int max_stages = std::min(TC_MAX_STAGES, (TC_SMEM_LIMIT - fixed) / per_stage);
+  p.nstages = max_stages;
   if (sims[0].tune.stages > 0) p.nstages = std::min(p.nstages, sims[0].tune.stages);
-  if (p.nstages < 2) return cudaErrorInvalidConfiguration;
   // A team waits on a stage's barriers by phase parity, which tells apart
   // only consecutive phases: a team may run at most one round of a stage
   // ahead of the MMAs, which holds while the teams are no more than the
   // stages (each team's previous stage was released before it).  Small
-  // teams of one-slot launches are widened until that holds.
+  // teams of one-slot launches are widened, and a stage cap below the
+  // number of teams raised, until that holds.
   while (TC_GEN_WARPS / p.team_warps > p.nstages && p.team_warps < TC_TEAM_WARPS)
     p.team_warps *= 2;
-  const int cl_team = kTeam16 ? 16 : TC_TEAM_WARPS;
-  if (TC_GEN_WARPS / p.team_warps > p.nstages || TC_GEN_WARPS / cl_team > p.nstages ||
-      TC_GEN_WARPS / p.team_warps > TC_NREC)
+  const int teams = std::max(TC_GEN_WARPS / p.team_warps, cluster ? TC_GEN_WARPS / TC_TEAM_WARPS : 1);
+  p.nstages = std::min(max_stages, std::max(p.nstages, teams));
+  if (p.nstages < 2 || teams > p.nstages || TC_GEN_WARPS / p.team_warps > TC_NREC)
     return cudaErrorInvalidConfiguration;
   const int smem = fixed + p.nstages * per_stage;
   e = tc_configure();
@@ -1461,10 +1495,10 @@ cudaError_t launch_form(const TcSimDesc* sims, int nsims, const void* rec, long 
   static int cached_n[2][TC_MAX_CLUSTER + 1][TC_MAX_STAGES + 1] = {};
   int& nclusters = cached_n[table][C][p.nstages];
   if (nclusters == 0) {
-    e = table ? cudaOccupancyMaxActiveClusters(&nclusters, tc_vis_kernel<true, true, kForm, kTeam16>,
+    e = table ? cudaOccupancyMaxActiveClusters(&nclusters, tc_vis_kernel<true, true, kForm>,
                                                &cfg)
               : cudaOccupancyMaxActiveClusters(&nclusters,
-                                               tc_vis_kernel<true, false, kForm, kTeam16>, &cfg);
+                                               tc_vis_kernel<true, false, kForm>, &cfg);
     if (e != cudaSuccess) return e;
   }
   if (nclusters < 1) return cudaErrorInvalidConfiguration;
@@ -1489,7 +1523,7 @@ cudaError_t launch_form(const TcSimDesc* sims, int nsims, const void* rec, long 
     p.split = share->d_split;
     p.split_side = 0;
     cfg.stream = share->hi;
-    if ((e = cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, false, kForm, kTeam16>, map, p)) !=
+    if ((e = cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, false, kForm>, map, p)) !=
         cudaSuccess)
       return e;
     TcParams q = p;
@@ -1505,8 +1539,8 @@ cudaError_t launch_form(const TcSimDesc* sims, int nsims, const void* rec, long 
     share->launched = 4;
     return cudaSuccess;
   }
-  e = table ? cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, true, kForm, kTeam16>, map, p)
-            : cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, false, kForm, kTeam16>, map, p);
+  e = table ? cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, true, kForm>, map, p)
+            : cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, false, kForm>, map, p);
   if (e != cudaSuccess) return e;
   if (share) share->launched = 1;
   return cudaGetLastError();
@@ -1526,15 +1560,12 @@ cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, l
   if (sims[0].form == 1) {
     for (int i = 0; i < nsims; ++i)
       if (!sims[i].sbound) return cudaErrorInvalidValue;
-    if (sims[0].tune.team_warps == 16)
-      return launch_form<1, true>(sims, nsims, rec, rec_rows, d_table, h_table, err, num_sms, st,
-                                  wait_ns, stall, share);
-    return launch_form<1, false>(sims, nsims, rec, rec_rows, d_table, h_table, err, num_sms, st,
-                                 wait_ns, stall, share);
+    return launch_form<1>(sims, nsims, rec, rec_rows, d_table, h_table, err, num_sms, st,
+                          wait_ns, stall, share);
   }
   if (sims[0].form != 0) return cudaErrorInvalidValue;
-  return launch_form<0, false>(sims, nsims, rec, rec_rows, d_table, h_table, err, num_sms, st,
-                               wait_ns, stall, share);
+  return launch_form<0>(sims, nsims, rec, rec_rows, d_table, h_table, err, num_sms, st,
+                        wait_ns, stall, share);
 }
 
 size_t tc_partial_floats(int Np, int nsrc, int nslices, int chunk) {

@@ -138,14 +138,12 @@ int hv_set_wait_limit(hv_context* ctx, uint64_t wait_ns, int stall);
  * batched form takes the same knobs from its autotuner).  No counterpart in
  * the reference, whose launch geometry is a fixed formula (vis.py:176-180).
  * value 0 restores the default of `param`:
- *   HV_TUNE_TEAM_WARPS  8 (default): two teams of 8 generator warps take
- *                       alternate stages; 16: one team per stage
- *                       (HV_METHOD_TC_FP16 on 129-1024 antennas only; other
- *                       calls ignore it)
  *   HV_TUNE_STAGES      cap on the operand stages held in shared memory,
- *                       2..8 (default: as many as fit) */
+ *                       2..8 (default: as many as fit; never below the
+ *                       number of generator teams).  Fewer stages leave more
+ *                       of the SM's on-chip memory to the L1 cache that
+ *                       serves the beam gathers. */
 enum {
-  HV_TUNE_TEAM_WARPS = 1,
   HV_TUNE_STAGES = 2
 };
 int hv_set_tuning(hv_context* ctx, int param, int value);

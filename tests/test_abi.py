@@ -117,7 +117,7 @@ def test_entry_points_reject_a_null_context(lib):
     assert lib.hv_set_profiling(None, 1) == ARG
     assert lib.hv_profile_read(None, ctypes.byref(d), ctypes.byref(u)) == ARG
     assert lib.hv_set_wait_limit(None, 0, 0) == ARG
-    assert lib.hv_set_tuning(None, 1, 0) == ARG
+    assert lib.hv_set_tuning(None, 2, 0) == ARG
     assert lib.hv_device_alloc(None, 16, ctypes.byref(p)) == ARG
     assert lib.hv_device_free(None, None) == ARG
     assert lib.hv_memcpy_async(None, None, None, 0, 1) == ARG
@@ -211,7 +211,6 @@ def test_python_constants_match_the_header():
     assert _native.METHODS["plain"] == header_enum("HV_METHOD_PLAIN")
     assert _native.METHODS["tc"] == _native.METHODS["tc_bf16"] == header_enum("HV_METHOD_TC_BF16")
     assert _native.METHODS["tc_fp16"] == header_enum("HV_METHOD_TC_FP16")
-    assert _native.HV_TUNE_TEAM_WARPS == header_enum("HV_TUNE_TEAM_WARPS")
     assert _native.HV_TUNE_STAGES == header_enum("HV_TUNE_STAGES")
 
 

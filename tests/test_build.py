@@ -3,11 +3,13 @@ flags (``nvcc -Xptxas -v``; it cross-compiles for sm_103a, no GPU is used).
 
 * Every kernel but the fused visibility kernel keeps its values in
   registers: no spills.
-* ``tc_vis_kernel`` runs 19 warps on the SM's 4 schedulers, so a thread may
-  hold 96 registers; its ten variants (cluster / one-CTA x batched / single
-  simulation x split-BF16 / FP16 + FP8 form, and the FP16 + FP8 cluster
-  variants with one 16-warp generator team) spill 96-140 bytes a thread, and
-  a change that spills more would slow its latency-bound phasor generators.
+* ``tc_vis_kernel`` has eight variants: cluster / one-CTA x batched /
+  single simulation x split-BF16 / FP16 + FP8 form.  The split-BF16 form
+  runs 15 warps, at most 4 on each of the SM's 4 schedulers, so a thread may
+  hold 128 registers, and spills at most 64 bytes; the FP16 + FP8 form runs
+  19 warps, so the busiest scheduler holds 5 and a thread 96 registers, and
+  spills 96-150 bytes.  A change that spills more would slow the
+  latency-bound phasor generators.
 """
 import concurrent.futures as cf
 import glob
@@ -44,7 +46,7 @@ def reports(tmp_path_factory):
 def test_every_source_reports_its_kernels(reports):
     assert set(reports) >= {"hv_tc.cu", "hv_plain.cu", "hv_prep.cu", "hv_omnical.cu",
                             "hv_median.cu", "hv_batch.cu"}
-    assert len([k for k in reports["hv_tc.cu"] if "tc_vis_kernel" in k]) == 10
+    assert len([k for k in reports["hv_tc.cu"] if "tc_vis_kernel" in k]) == 8
 
 
 def test_no_kernel_but_the_fused_one_spills(reports):
@@ -56,5 +58,6 @@ def test_no_kernel_but_the_fused_one_spills(reports):
 def test_fused_kernel_register_budget(reports):
     for name, (stores, loads, regs) in reports["hv_tc.cu"].items():
         if "tc_vis_kernel" in name:
-            assert regs <= 96, (name, regs)
-            assert stores <= 144, (name, stores)
+            split_bf16 = "Li0E" in name   # the form template argument, 0 = split BF16
+            assert regs <= (128 if split_bf16 else 96), (name, regs)
+            assert stores <= (64 if split_bf16 else 152), (name, stores)

@@ -218,8 +218,9 @@ def test_fp16_form_scales_each_slice():
         assert rel_frobenius(v[f], ref).max() <= 1e-4, f
 
 
-@pytest.mark.parametrize("team_warps,stages", [(16, 0), (8, 2), (16, 2)])
-def test_fp16_launch_shapes_agree(team_warps, stages):
+@pytest.mark.parametrize("method", ["tc", "tc_fp16"])
+@pytest.mark.parametrize("stages", [2, 3, 4])
+def test_launch_shapes_agree(method, stages):
     # the tuning knobs change how the work is laid out on the SM, not the
     # arithmetic: every shape gives the default's result bit for bit
     from hera_gpu_gb300 import _native
@@ -228,9 +229,9 @@ def test_fp16_launch_shapes_agree(team_warps, stages):
     bms = synth.beams_for(cfg, dtype=np.float32)
     args = (cfg["antpos"], cfg["freqs"], cfg["eq2tops"], cfg["crd_eq"], cfg["I_sky"], bms)
     ctx = _native.Context(0)
-    ref = vis_gpu_multifreq(*args, precision=1, method="tc_fp16", context=ctx)
-    ctx.set_tuning(team_warps=team_warps, stages=stages)
-    got = vis_gpu_multifreq(*args, precision=1, method="tc_fp16", context=ctx)
+    ref = vis_gpu_multifreq(*args, precision=1, method=method, context=ctx)
+    ctx.set_tuning(stages=stages)
+    got = vis_gpu_multifreq(*args, precision=1, method=method, context=ctx)
     np.testing.assert_array_equal(got, ref)
 
 
