@@ -678,6 +678,20 @@ __device__ __forceinline__ void gen_unit(const SrcRec32* rec, const Ucoef32& uc,
 }
 
 // ------------------------------------------------------------- the kernel --
+// Position of a global stage counter in the ring of NS operand stages (slot
+// and phase parity), moved forward without dividing by the runtime NS.
+struct StageRing {
+  uint32_t s = 0, ph = 0;
+  __device__ __forceinline__ void advance(uint32_t by, uint32_t ns) {  // by <= ns
+    s += by;
+    if (s >= ns) {
+      s -= ns;
+      ph ^= 1u;
+    }
+  }
+};
+static_assert((TC_NREC & (TC_NREC - 1)) == 0, "the record ring is indexed by masks");
+
 struct ItemInfo {
   const TcSim* sim;
   int g, k, tl, f, sl;
@@ -851,6 +865,10 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
     const int nteams = TC_GEN_WARPS / team_warps;
     const int team = warp / team_warps;  // takes the stages with gs % nteams == team
     uint32_t gs = 0, ic = 0;
+    // this team's next stage (global counter) and its operand-ring position
+    uint32_t my_gs = (uint32_t)team;
+    StageRing ring;
+    ring.advance((uint32_t)team, (uint32_t)NS);
     ItemInfo d;
     for (long long it = it0; it < it_end; it += istep) {
       if (!decode_item<kCluster, kTable, KS>(p, it, rank, d)) continue;
@@ -910,12 +928,15 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       for (int j0 = 0; j0 < d.nst && ok; j0 += FLUSH) {
         const int j1 = min(d.nst, j0 + FLUSH);
         const int jend = min(d.nst, j1 + ahead);
-        for (int j = jdone; j < jend && ok && generates; ++j, ++gs) {
-          if ((int)(gs % (uint32_t)nteams) != team) continue;  // another team's stage
-          const int s = (int)(gs % NS);
-          const uint32_t par = (gs / NS) & 1;
-          const int rs = (int)(gs % TC_NREC);
-          if (!wait_warp(rec_full(rs), (gs / TC_NREC) & 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
+        // this team's stages of [jdone, jend): global stages gs + (j - jdone)
+        // with gs % nteams == team
+        const uint32_t gs_end = gs + (uint32_t)(jend - jdone);
+        for (; my_gs < gs_end && ok && generates;
+             my_gs += (uint32_t)nteams, ring.advance((uint32_t)nteams, (uint32_t)NS)) {
+          const int s = (int)ring.s;
+          const uint32_t par = ring.ph;
+          const int rs = (int)(my_gs & (TC_NREC - 1));
+          if (!wait_warp(rec_full(rs), (my_gs / TC_NREC) & 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
           if (!wait_warp<kCluster>(smem_empty(s), par ^ 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
           const SrcRec32* recs = reinterpret_cast<const SrcRec32*>(rec_smem + (size_t)rs * REC);
           const uint32_t stage_op = op_base + (uint32_t)s * stage_bytes;
@@ -982,6 +1003,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
             mbar_arrive(rec_empty(rs));  // the records may be reloaded
           }
         }
+        gs = gs_end;
         if (!ok) break;
         jdone = jend;
         // ------------------------------------------------------- epilogue --
@@ -1057,7 +1079,7 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       for (long long it = it0; it < it_end && ok; it += istep) {
         if (!decode_item<kCluster, kTable, KS>(p, it, rank, d)) continue;
         for (int j = 0; j < d.nst; ++j, ++gs) {
-          const int r = (int)(gs % TC_NREC);
+          const int r = (int)(gs & (TC_NREC - 1));
           const uint32_t par = (gs / TC_NREC) & 1;
           // this CTA's generators have finished reading the previous round
           if (!wait1(rec_empty(r), par ^ 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
@@ -1071,12 +1093,13 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       // let the copies still in flight land before the CTA can exit
       const uint32_t first = gs > (uint32_t)TC_NREC ? gs - TC_NREC : 0;
       for (uint32_t g = first; g < gs; ++g)
-        wait_drain(rec_full((int)(g % TC_NREC)), (g / TC_NREC) & 1, p.err, p.wait_ns);
+        wait_drain(rec_full((int)(g & (TC_NREC - 1))), (g / TC_NREC) & 1, p.err, p.wait_ns);
     }
   } else if (warp == TC_MMA_WARP) {
     // ------------------------------------------------------- MMA issuer --
     if (lane == 0) {
-      uint32_t gs = 0, ic = 0;
+      uint32_t ic = 0;
+      StageRing ring;  // operand stage of the next MMA
       ItemInfo d;
       bool ok = true;
       const uint16_t cmask = kCluster ? (uint16_t)__ldg(&mine->commit_mask) : (uint16_t)1;
@@ -1093,9 +1116,9 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
           // the generators have read the accumulator of the last flush
           if (!wait1(acc_empty, (ic & 1) ^ 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
           tc_fence_after();
-          for (int j = j0; j < j1; ++j, ++gs) {
-            const int s = (int)(gs % NS);
-            const uint32_t par = (gs / NS) & 1;
+          for (int j = j0; j < j1; ++j, ring.advance(1u, (uint32_t)NS)) {
+            const int s = (int)ring.s;
+            const uint32_t par = ring.ph;
             if (!wait1(smem_full(s), par, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
             // arm the next round of this stage for the peers' pushes (they can
             // only come after this round's MMAs release the slot)
@@ -1127,14 +1150,14 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
 
   if (kCluster && warp == TC_PUSH_WARP && lane == 0 && nown > 0) {
     // ---------------------------------------------- DSMEM tile pusher --
-    uint32_t gs = 0;
+    StageRing ring;  // operand stage of the next push
     ItemInfo d;
     bool ok = true;
     for (long long it = it0; it < it_end && ok; it += istep) {
       if (!decode_item<kCluster, kTable, KS>(p, it, rank, d)) continue;
-      for (int j = 0; j < d.nst; ++j, ++gs) {
-        const int s = (int)(gs % NS);
-        const uint32_t par = (gs / NS) & 1;
+      for (int j = 0; j < d.nst; ++j, ring.advance(1u, (uint32_t)NS)) {
+        const int s = (int)ring.s;
+        const uint32_t par = ring.ph;
         if (!wait1(gen_done(s), par, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
         const uint32_t stage_op = op_base + (uint32_t)s * stage_bytes;
         for (int k = 0; k < nown; ++k) {
