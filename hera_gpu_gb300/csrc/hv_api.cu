@@ -53,6 +53,7 @@ struct hv_context {
   std::string err;
   uint64_t launches = 0;
   int* d_err = nullptr;  // device-side error flag (bounded waits)
+  unsigned long long* d_claim = nullptr;  // item-claim counter of the fused launches
   // profiling of the visibility-product kernels
   bool profiling = false;
   // device-side wait limit of the fused kernel (0: its default) and fault
@@ -317,8 +318,8 @@ int run_device(hv_context* ctx, int method, const R* antpos, int nant, const dou
         if (nsrc > 0)
           HV_LAUNCH_TIMED(launch_tc_batch(&L, 1, ctx->rec.p, (long long)nt * rec_stride,
                                           ctx->tctable.p, ctx->tctable_h.p, ctx->d_err,
-                                          ctx->num_sms, st, ctx->wait_ns, ctx->stall,
-                                          &ctx->share),
+                                          ctx->d_claim, ctx->num_sms, st, ctx->wait_ns,
+                                          ctx->stall, &ctx->share),
                           st);
         if (nsrc > 0 && ctx->share.launched > 1) ctx->launches += ctx->share.launched - 1;
         HV_LAUNCH(1, launch_reduce<float>(static_cast<float*>(ctx->partial.p), slice_floats,
@@ -454,10 +455,11 @@ int hv_create(hv_context** out, int device, size_t hbm_budget_bytes) {
     ctx->cc_major = prop.major;
     ctx->cc_minor = prop.minor;
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { r = HV_ERR_CUDA; break; }
-    // device error flag and the split point of shared fused launches
-    if (cudaMalloc(&ctx->d_err, 2 * sizeof(int)) != cudaSuccess) { r = HV_ERR_OOM; break; }
-    if (cudaMemset(ctx->d_err, 0, 2 * sizeof(int)) != cudaSuccess) { r = HV_ERR_CUDA; break; }
-    ctx->share.d_split = ctx->d_err + 1;
+    // device error flag (int) and the item-claim counter of the fused
+    // launches (8 bytes, at offset 8)
+    if (cudaMalloc(&ctx->d_err, 16) != cudaSuccess) { r = HV_ERR_OOM; break; }
+    if (cudaMemset(ctx->d_err, 0, 16) != cudaSuccess) { r = HV_ERR_CUDA; break; }
+    ctx->d_claim = reinterpret_cast<unsigned long long*>(ctx->d_err + 2);
     int least = 0, greatest = 0;
     if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess ||
         cudaStreamCreateWithPriority(&ctx->share.hi, cudaStreamNonBlocking, greatest) != cudaSuccess ||

@@ -60,7 +60,8 @@ struct hv_batch {
   void* host = nullptr;                    // pinned: frequencies, group tables, sim tables
   size_t host_cap = 0;                     // its size (a block of the context's pool)
   size_t host_bytes = 0, h_table = 0, h_groups = 0;
-  int* d_err = nullptr;
+  int* d_err = nullptr;                    // error flag (int) and, at offset 8, the
+  unsigned long long* d_claim = nullptr;   // item-claim counter of its fused launches
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::string err;
@@ -233,9 +234,9 @@ int enqueue(hv_batch* b, cudaStream_t st, int timed_class = -1) {
       nl += 3;
     }
   }
-  // one persistent fused launch per class; its items are handed out
-  // round-robin in table order, so the simulations with the largest items
-  // go first and the small ones fill the tail
+  // one persistent fused launch per class; its CTAs claim the items in
+  // table order, so the simulations with the largest items go first and the
+  // small ones fill the tail
   size_t toff = 0;
   for (size_t c = 0; c < b->classes.size(); ++c) {
     std::vector<int> order = b->classes[c];
@@ -283,8 +284,8 @@ int enqueue(hv_batch* b, cudaStream_t st, int timed_class = -1) {
       TcShare* share = d.size() == 1 && timed_class < 0 ? hv_context_share(b->ctx) : nullptr;
       HB_CK(launch_tc_batch(d.data(), (int)d.size(), b->rec, b->rec_rows,
                             static_cast<char*>(b->table) + toff, H + b->h_table + toff, b->d_err,
-                            b->num_sms, st, hv_context_wait_ns(b->ctx), hv_context_stall(b->ctx),
-                            share));
+                            b->d_claim, b->num_sms, st, hv_context_wait_ns(b->ctx),
+                            hv_context_stall(b->ctx), share));
       if (share && share->launched > 1) nl += share->launched - 1;
       if (prof) {
         HB_CK(cudaEventRecord(e1, st));
@@ -334,9 +335,10 @@ int hv_batch_create(hv_context* ctx, const hv_sim* sims, int nsims, unsigned fla
   do {
     if (cudaGetDevice(&b->device) != cudaSuccess) { r = HV_ERR_CUDA; break; }
     b->num_sms = hv_context_num_sms(ctx);
-    if (cudaMallocAsync(reinterpret_cast<void**>(&b->d_err), sizeof(int), hv_context_stream(ctx)) !=
+    if (cudaMallocAsync(reinterpret_cast<void**>(&b->d_err), 16, hv_context_stream(ctx)) !=
         cudaSuccess) { r = HV_ERR_OOM; break; }
-    cudaMemsetAsync(b->d_err, 0, sizeof(int), hv_context_stream(ctx));
+    cudaMemsetAsync(b->d_err, 0, 16, hv_context_stream(ctx));
+    b->d_claim = reinterpret_cast<unsigned long long*>(b->d_err + 2);
     std::map<int, int> class_of;  // cluster size (0 = no cluster) -> class
     for (int i = 0; i < nsims; ++i) {
       r = check_sim(b, sims[i], i);

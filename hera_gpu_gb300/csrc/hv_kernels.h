@@ -123,7 +123,9 @@ int tc_num_groups(int nant);
 int tc_team_warps(int nant);
 // One-time launch attributes of the fused kernel (call outside stream capture).
 cudaError_t tc_configure();
-// All items of nsims simulations in one persistent launch.  rec: SrcRec32
+// All items of nsims simulations in one persistent launch; its CTAs claim
+// the items at run time from *claim (8 bytes of device memory that no other
+// launch uses at the same time; zeroed here, in stream order).  rec: SrcRec32
 // rows (rewritten by launch_tc_relative) of every simulation, rec_rows in
 // all.  d_table / h_table: device and host (kept alive until the copy ran)
 // buffers of tc_sim_table_bytes(nsims).  Cluster mode is used when every
@@ -136,13 +138,12 @@ cudaError_t tc_configure();
 struct TcShare {
   cudaStream_t hi, lo;                  // highest- and lowest-priority streams
   cudaEvent_t fork, join_hi, join_lo;   // timing disabled
-  int* d_split;                         // device int: the split point
   int launched;
 };
 cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, long long rec_rows,
-                            void* d_table, void* h_table, int* err, int num_sms,
-                            cudaStream_t st, unsigned long long wait_ns = 0, int stall = 0,
-                            TcShare* share = nullptr);
+                            void* d_table, void* h_table, int* err, unsigned long long* claim,
+                            int num_sms, cudaStream_t st, unsigned long long wait_ns = 0,
+                            int stall = 0, TcShare* share = nullptr);
 size_t tc_partial_floats(int Np, int nsrc, int nslices, int chunk);
 int tc_chunk_sources(int nsrc, int nslices, int ngroups, int num_sms);
 size_t tc_group_table_bytes(int nant);

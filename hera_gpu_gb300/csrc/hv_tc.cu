@@ -75,6 +75,7 @@
 #include <cuda_fp8.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "hv_internal.cuh"
@@ -199,13 +200,26 @@ struct TcParams {
   int* err;
   unsigned long long wait_ns;  // limit of one wait
   int stall;                   // fault injection: the first record copy is never issued
-  // Shared launch of one simulation (split != null): the cluster launch runs
-  // the cluster items [0, *split), a one-CTA-per-item launch on the SMs no
-  // cluster fits on runs the group items [*split * ngroups, total_items).
-  const int* split;
-  int split_side;  // 0: the cluster launch, 1: the one-CTA launch
-  int team_warps;  // generator warps per stage without clusters (8, or 4 / 2 for small groups)
+  // Items are claimed at run time from *claim (zero before the launch):
+  //  kClaimCount  one counter of the launch's own items (total_items);
+  //  kClaimFront  shared launch of one simulation, its cluster kernel: whole
+  //               cluster items from the front of the packed word (high 32
+  //               bits: cluster items taken), while none of their group
+  //               items has been taken from the back;
+  //  kClaimBack   the one-CTA kernel of that shared launch, on the SMs no
+  //               cluster fits on: group items (cluster item x ngroups +
+  //               group) from the back (low 32 bits: group items taken),
+  //               down to the front's last claim.
+  // Every item is computed exactly once, whichever kernel starts first.
+  unsigned long long* claim;
+  int claim_mode;
+  long long group_items;  // shared launch: cluster items x ngroups
+  int team_warps;  // generator warps per stage without clusters (a full team, or 1/2 or 1/4)
 };
+constexpr int kClaimCount = 0, kClaimFront = 1, kClaimBack = 2;
+// Items a CTA has claimed ahead of its slowest role (the ring of item
+// indices in shared memory).
+constexpr int TC_ITEM_RING = 4;
 
 // Read-only load of a pointer-valued field.
 template <typename T>
@@ -322,6 +336,9 @@ __device__ __forceinline__ void sts128_cluster(uint32_t addr, uint4 v) {
   asm volatile("st.shared::cluster.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x),
                "r"(v.y), "r"(v.z), "r"(v.w)
                : "memory");
+}
+__device__ __forceinline__ void st_cluster_b64(uint32_t addr, long long v) {
+  asm volatile("st.shared::cluster.b64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
 }
 __device__ __forceinline__ void mbar_arrive_cluster(uint32_t remote_bar) {
   asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(remote_bar)
@@ -692,6 +709,29 @@ struct StageRing {
 };
 static_assert((TC_NREC & (TC_NREC - 1)) == 0, "the record ring is indexed by masks");
 
+// The next item of this CTA (or cluster), or -1 when the launch's items are
+// all taken (see TcParams::claim).
+__device__ __forceinline__ long long claim_item(const TcParams& p) {
+  if (p.claim_mode == kClaimCount) {
+    const unsigned long long x = atomicAdd(p.claim, 1ull);
+    return x < (unsigned long long)p.total_items ? (long long)x : -1;
+  }
+  const unsigned long long C = (unsigned long long)p.one.ngroups;
+  const unsigned long long G = (unsigned long long)p.group_items;
+  volatile unsigned long long* w = p.claim;
+  for (;;) {
+    const unsigned long long old = *w;
+    const unsigned long long f = old >> 32, b = old & 0xffffffffull;
+    if (p.claim_mode == kClaimFront) {
+      if ((f + 1) * C + b > G) return -1;  // its groups reach the back's claims
+      if (atomicCAS(p.claim, old, old + (1ull << 32)) == old) return (long long)f;
+    } else {
+      if (f * C + b >= G) return -1;       // the front took the rest
+      if (atomicCAS(p.claim, old, old + 1ull) == old) return (long long)(G - 1 - b);
+    }
+  }
+}
+
 struct ItemInfo {
   const TcSim* sim;
   int g, k, tl, f, sl;
@@ -796,7 +836,15 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
   const uint32_t acc_full = sbar0 + 8u * (3 * NS);
   const uint32_t acc_empty = acc_full + 8;
   const uint32_t drain = acc_full + 16;
-  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2 * TC_NREC + 3 * NS + 3);
+  // ring of claimed item indices: written by the claiming thread (in
+  // cluster mode rank 0's, into every CTA of the cluster), read by every
+  // role; item_empty of the claiming CTA counts the reads of all CTAs
+  const uint32_t ibar0 = acc_full + 24;
+  auto item_full = [&](int k) { return ibar0 + 8u * k; };
+  auto item_empty = [&](int k) { return ibar0 + 8u * (TC_ITEM_RING + k); };
+  long long* item_ring = reinterpret_cast<long long*>(bars + 2 * TC_NREC + 3 * NS + 3 +
+                                                      2 * TC_ITEM_RING);
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(item_ring + TC_ITEM_RING);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -804,15 +852,8 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
   // cluster mode: every simulation of the launch has the same group layout
   // (one group per CTA of the cluster), so its barrier counts are common
   const int csize = kCluster ? (kTable ? (int)__ldg(&p.sims[0].ngroups) : p.one.ngroups) : 1;
-  long long it0 = kCluster ? blockIdx.x / csize : blockIdx.x;
-  const long long istep = kCluster ? gridDim.x / csize : gridDim.x;
-  long long it_end = p.total_items;
-  if (p.split) {
-    const long long x = *p.split;
-    if (p.split_side) it0 += x * p.one.ngroups;
-    else it_end = min(it_end, x);
-  }
-  const TcGroup* mine = (kTable ? ldg_ptr(&p.sims[0].groups) : p.one.groups) + rank;
+  const TcGroup* groups0 = kTable ? ldg_ptr(&p.sims[0].groups) : p.one.groups;
+  const TcGroup* mine = groups0 + rank;
   // cluster mode: operand bytes this CTA receives from peers per stage
   const uint32_t recv_bytes =
       kCluster ? (uint32_t)__ldg(&mine->recv_slots) * (uint32_t)(TILES * TC_SLOT) : 0u;
@@ -838,6 +879,21 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
     mbar_init(acc_full, 1);
     mbar_init(acc_empty, TC_GEN_THREADS);
     mbar_init(drain, 1);
+    // readers of each claimed item: every generator warp and the MMA thread
+    // of every CTA, the pusher and (but for the claimer's own) the producer
+    // of every generating CTA
+    int readers = TC_GEN_WARPS + 1;
+    if (kCluster && rank == 0) {
+      readers = 0;
+      for (int r = 0; r < csize; ++r) {
+        const int gen_r = __ldg(&groups0[r].nown) > 0;
+        readers += TC_GEN_WARPS + 1 + gen_r + (r != 0 && gen_r);
+      }
+    }
+    for (int k = 0; k < TC_ITEM_RING; ++k) {
+      mbar_init(item_full(k), 1);
+      mbar_init(item_empty(k), readers);
+    }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     // the first round of every stage expects the peers' pushed tiles
@@ -858,6 +914,26 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
   tc_fence_after();
   const uint32_t tmem = *tmem_holder;
 
+  // The k-th item of this CTA, read from the ring by one thread (or a whole
+  // warp, kWarp: every lane reads it), its slot then released to the
+  // claiming CTA; false if a wait gave up.
+  auto read_item = [&](uint32_t k, long long& it, auto warp_tag) -> bool {
+    constexpr bool kWarp = decltype(warp_tag)::value;
+    const int slot = (int)(k % TC_ITEM_RING);
+    const uint32_t par = (k / TC_ITEM_RING) & 1;
+    const bool got = kWarp ? wait_warp<kCluster>(item_full(slot), par, abort_flag, p.err, p.wait_ns)
+                           : wait1<kCluster>(item_full(slot), par, abort_flag, p.err, p.wait_ns);
+    if (!got) return false;
+    it = *reinterpret_cast<volatile long long*>(item_ring + slot);
+    if (!kWarp || lane == 0) {
+      if (kCluster) mbar_arrive_cluster(map_to_rank(item_empty(slot), 0));
+      else mbar_arrive(item_empty(slot));
+    }
+    return true;
+  };
+  using one_thread = std::integral_constant<bool, false>;
+  using whole_warp = std::integral_constant<bool, true>;
+
   if (warp < TC_GEN_WARPS) {
     // ------------------------------------------------ phasor generators --
     const int tid = threadIdx.x;
@@ -870,7 +946,9 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
     StageRing ring;
     ring.advance((uint32_t)team, (uint32_t)NS);
     ItemInfo d;
-    for (long long it = it0; it < it_end; it += istep) {
+    for (uint32_t k = 0;; ++k) {
+      long long it;
+      if (!read_item(k, it, whole_warp{}) || it < 0) break;
       if (!decode_item<kCluster, kTable, KS>(p, it, rank, d)) continue;
       const TcGroup* gp = SIM_P(d, groups) + d.g;
       const int Np = SIM_I(d, Np), dx = SIM_I(d, dx), dy = SIM_I(d, dy);
@@ -1072,11 +1150,37 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
     }
   } else if (warp == TC_PRODUCER_WARP) {
     // ----------------------------------------------------- TMA producer --
-    if (lane == 0 && generates) {
+    // The claiming thread (this CTA's producer; in cluster mode rank 0's)
+    // takes the next item when it is about to load its records, so an item
+    // is held by a CTA only once that CTA is ready for it.
+    const bool claimer = rank == 0;
+    if (lane == 0 && (generates || claimer)) {
       uint32_t gs = 0;
       ItemInfo d;
       bool ok = true;
-      for (long long it = it0; it < it_end && ok; it += istep) {
+      for (uint32_t k = 0; ok; ++k) {
+        long long it;
+        if (claimer) {
+          const int slot = (int)(k % TC_ITEM_RING);
+          // every reader of every CTA has read the slot's previous item
+          if (!wait1<kCluster>(item_empty(slot), ((k / TC_ITEM_RING) & 1) ^ 1, abort_flag, p.err,
+                               p.wait_ns)) { ok = false; break; }
+          it = claim_item(p);
+          if (kCluster) {
+            for (int r = 0; r < csize; ++r) {
+              st_cluster_b64(map_to_rank(smem_u32(item_ring + slot), (uint32_t)r), it);
+              mbar_arrive_cluster(map_to_rank(item_full(slot), (uint32_t)r));
+            }
+          } else {
+            item_ring[slot] = it;
+            mbar_arrive(item_full(slot));  // release: the index is visible first
+          }
+        } else if (!read_item(k, it, one_thread{})) {
+          ok = false;
+          break;
+        }
+        if (it < 0) break;
+        if (!generates) continue;
         if (!decode_item<kCluster, kTable, KS>(p, it, rank, d)) continue;
         for (int j = 0; j < d.nst; ++j, ++gs) {
           const int r = (int)(gs & (TC_NREC - 1));
@@ -1103,7 +1207,9 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
       ItemInfo d;
       bool ok = true;
       const uint16_t cmask = kCluster ? (uint16_t)__ldg(&mine->commit_mask) : (uint16_t)1;
-      for (long long it = it0; it < it_end && ok; it += istep) {
+      for (uint32_t k = 0; ok; ++k) {
+        long long it;
+        if (!read_item(k, it, one_thread{}) || it < 0) break;
         if (!decode_item<kCluster, kTable, KS>(p, it, rank, d)) continue;
         const TcGroup* gp = SIM_P(d, groups) + d.g;
         const int nm = __ldg(&gp->n_mma);
@@ -1153,7 +1259,9 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
     StageRing ring;  // operand stage of the next push
     ItemInfo d;
     bool ok = true;
-    for (long long it = it0; it < it_end && ok; it += istep) {
+    for (uint32_t k = 0; ok; ++k) {
+      long long it;
+      if (!read_item(k, it, one_thread{}) || it < 0) break;
       if (!decode_item<kCluster, kTable, KS>(p, it, rank, d)) continue;
       for (int j = 0; j < d.nst; ++j, ring.advance(1u, (uint32_t)NS)) {
         const int s = (int)ring.s;
@@ -1192,26 +1300,6 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
 
 #undef SIM_I
 #undef SIM_P
-
-// Holds back the next launch on its stream by `ns` nanoseconds (one thread
-// timing itself; it waits on nothing else): the one-CTA launch of a shared
-// launch must not take SMs before the cluster launch has placed its clusters.
-__global__ void tc_hold_kernel(unsigned long long ns) {
-  const unsigned long long t0 = global_ns();
-  while (global_ns() - t0 < ns) __nanosleep(1000);
-}
-
-// Where a shared launch of one simulation splits its items: the cluster
-// launch keeps the first (1 - side_frac) of the cluster items that hold
-// sources above the horizon (the decode order of decode_item).
-__global__ void tc_split_kernel(const int* __restrict__ counts, int nt, int nf, int chunk,
-                                float side_frac, int* __restrict__ split) {
-  if (threadIdx.x != 0) return;
-  long long n = 0;
-  for (int t = 0; t < nt; ++t) n += (long long)((counts[t] + chunk - 1) / chunk) * nf;
-  const long long side = (long long)ceilf(side_frac * (float)n);
-  *split = (int)(n - min(side, n));
-}
 
 // ------------------------------------------------------------------- host --
 namespace {
@@ -1400,8 +1488,9 @@ namespace {
 // The launches of one fused-kernel call in form kForm (see launch_tc_batch).
 template <int kForm>
 cudaError_t launch_form(const TcSimDesc* sims, int nsims, const void* rec, long long rec_rows,
-                        void* d_table, void* h_table, int* err, int num_sms, cudaStream_t st,
-                        unsigned long long wait_ns, int stall, TcShare* share) {
+                        void* d_table, void* h_table, int* err, unsigned long long* claim,
+                        int num_sms, cudaStream_t st, unsigned long long wait_ns, int stall,
+                        TcShare* share) {
   constexpr int KS = TcForm<kForm>::KS;
   constexpr int TILES = TcForm<kForm>::TILES;
   constexpr int TC_GEN_WARPS = TcLayout<kForm>::GEN_WARPS;
@@ -1463,7 +1552,12 @@ cudaError_t launch_form(const TcSimDesc* sims, int nsims, const void* rec, long 
     if (e != cudaSuccess) return e;
   }
 
+  // the claim counter starts at zero (in stream order, before the launches)
+  e = cudaMemsetAsync(claim, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
   TcParams p{};
+  p.claim = claim;
+  p.claim_mode = kClaimCount;
   p.sims = static_cast<const TcSim*>(d_table);
   p.one = tab[0];
   p.nsims = nsims;
@@ -1529,37 +1623,33 @@ cudaError_t launch_form(const TcSimDesc* sims, int nsims, const void* rec, long 
   cfg.gridDim = dim3((unsigned)(C * ncl));
   const int leftover = num_sms - C * ncl;
   if (share && !table && leftover >= 4) {
-    // The SMs no cluster fits on take a share of the items, one CTA per group
-    // item: a one-CTA item runs at about 0.7 of a cluster CTA's rate (it
-    // generates all of its group's blocks itself; measured at 350 antennas).
-    // The cluster launch goes to the higher-priority stream so that its
-    // clusters are placed first.
-    const float r = 0.68f;
-    const float side_frac = leftover * r / (C * ncl + leftover * r);
-    const TcSimDesc& L = sims[0];
-    tc_split_kernel<<<1, 32, 0, st>>>(L.counts, L.nt, L.nf, L.chunk, side_frac, share->d_split);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    // The SMs no cluster fits on run the same items, one CTA per group item,
+    // in a second launch: the two claim from the two ends of one packed
+    // counter (kClaimFront / kClaimBack), so each item is computed once and
+    // the split adapts at run time (a one-CTA item, which generates all of
+    // its group's blocks itself, runs at about 0.7 of a cluster CTA's rate).
+    // The cluster launch goes to the higher-priority stream; should the
+    // one-CTA launch take an SM a cluster needed first, that cluster claims
+    // fewer items and nothing waits for it.
     if ((e = cudaEventRecord(share->fork, st)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(share->hi, share->fork, 0)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(share->lo, share->fork, 0)) != cudaSuccess) return e;
-    p.split = share->d_split;
-    p.split_side = 0;
+    p.claim_mode = kClaimFront;
+    p.group_items = items * C;
     cfg.stream = share->hi;
     if ((e = cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, false, kForm>, map, p)) !=
         cudaSuccess)
       return e;
     TcParams q = p;
     q.total_items = items * C;
-    q.split_side = 1;
-    tc_hold_kernel<<<1, 32, 0, share->lo>>>(100000ull);
+    q.claim_mode = kClaimBack;
     tc_vis_kernel<false, false, kForm><<<leftover, TC_THREADS, smem, share->lo>>>(map, q);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = cudaEventRecord(share->join_hi, share->hi)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(share->join_lo, share->lo)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(st, share->join_hi, 0)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(st, share->join_lo, 0)) != cudaSuccess) return e;
-    share->launched = 4;
+    share->launched = 2;
     return cudaSuccess;
   }
   e = table ? cudaLaunchKernelEx(&cfg, tc_vis_kernel<true, true, kForm>, map, p)
@@ -1572,8 +1662,8 @@ cudaError_t launch_form(const TcSimDesc* sims, int nsims, const void* rec, long 
 }  // namespace
 
 cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, long long rec_rows,
-                            void* d_table, void* h_table, int* err, int num_sms,
-                            cudaStream_t st, unsigned long long wait_ns, int stall,
+                            void* d_table, void* h_table, int* err, unsigned long long* claim,
+                            int num_sms, cudaStream_t st, unsigned long long wait_ns, int stall,
                             TcShare* share) {
   if (share) share->launched = 0;
   if (nsims <= 0 || rec_rows <= 0) return cudaSuccess;
@@ -1583,11 +1673,11 @@ cudaError_t launch_tc_batch(const TcSimDesc* sims, int nsims, const void* rec, l
   if (sims[0].form == 1) {
     for (int i = 0; i < nsims; ++i)
       if (!sims[i].sbound) return cudaErrorInvalidValue;
-    return launch_form<1>(sims, nsims, rec, rec_rows, d_table, h_table, err, num_sms, st,
+    return launch_form<1>(sims, nsims, rec, rec_rows, d_table, h_table, err, claim, num_sms, st,
                           wait_ns, stall, share);
   }
   if (sims[0].form != 0) return cudaErrorInvalidValue;
-  return launch_form<0>(sims, nsims, rec, rec_rows, d_table, h_table, err, num_sms, st,
+  return launch_form<0>(sims, nsims, rec, rec_rows, d_table, h_table, err, claim, num_sms, st,
                         wait_ns, stall, share);
 }
 
