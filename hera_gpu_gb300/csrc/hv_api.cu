@@ -380,6 +380,10 @@ int check_err_flag(hv_context* ctx) {
                   "antenna positions x frequency exceed the FP32 phase range of the tensor-core "
                   "method (|U| >= 4e6 cycles); results of the last call are invalid, use the "
                   "plain method");
+    if (flag == 3)
+      return fail(ctx, HV_ERR_UNSUPPORTED,
+                  "the fused kernel's dynamic shared memory is not 1024-byte aligned on this "
+                  "device; results of the last call are invalid, use the plain method");
     return fail(ctx, HV_ERR_TIMEOUT,
                 "a device-side wait gave up (code %d); results of the last call are invalid", flag);
   }

@@ -458,7 +458,7 @@ int hv_batch_sync(hv_batch* b) {
     return HV_ERR_CUDA;
   if (flag) {
     cudaMemsetAsync(b->d_err, 0, sizeof(int), st);
-    return flag == 2 ? HV_ERR_ARG : HV_ERR_TIMEOUT;
+    return flag == 2 ? HV_ERR_ARG : flag == 3 ? HV_ERR_UNSUPPORTED : HV_ERR_TIMEOUT;
   }
   return HV_OK;
 }

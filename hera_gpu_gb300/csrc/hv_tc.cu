@@ -87,19 +87,22 @@ constexpr int TC_ROWS = 128;          // antennas per block = MMA M
 constexpr int TC_SLOT = 16384;        // one operand tile: 128 rows x 128 B
 // Sources per stage: 16 for split BF16 (one tile per slot: hi and lo of 16
 // sources), 32 for FP16 + FP8 (two tiles per slot, see above).
+// Record stages: at least the operand stages (TC_MAX_STAGES), which makes
+// every phase-parity wait on a record barrier exact (see the generators).
+constexpr int TC_NREC_ALL = 8;
 template <int kForm> struct TcForm;
 template <> struct TcForm<0> {
-  static constexpr int KS = 16, TILES = 1;
+  static constexpr int KS = 16, TILES = 1, NREC = TC_NREC_ALL;
 };
 template <> struct TcForm<1> {
-  static constexpr int KS = 32, TILES = 2;
+  static constexpr int KS = 32, TILES = 2, NREC = TC_NREC_ALL;
 };
 constexpr int TC_KS_MAX = 32;
 constexpr int TC_REC_MAX = TC_KS_MAX * 32;  // bytes of source records per stage (largest form)
 // Record stages: more than operand stages (they are small), so the TMA
 // producer runs further ahead and a generator warp finds its next records
 // loaded even while slower warps still hold earlier stages.
-constexpr int TC_NREC = 8;
+
 // Warp layout of each form.  The SM's four schedulers each hold a quarter
 // of the block's warps, and a scheduler's 16K-register file is shared by
 // its warps.
@@ -138,6 +141,7 @@ constexpr int TC_MAX_STAGES = 8;
 #ifndef TC_FLUSH_SOURCES
 #define TC_FLUSH_SOURCES 2048
 #endif
+static_assert(TC_MAX_STAGES <= TC_NREC_ALL, "record stages >= operand stages");
 static_assert(TC_FLUSH_SOURCES % TC_KS_MAX == 0, "flush interval: whole stages of every form");
 constexpr int TC_TMEM_COLS = 512;
 constexpr int TC_SMEM_LIMIT = 227 * 1024;
@@ -145,6 +149,7 @@ constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // default limit of on
 
 constexpr int kErrTimeout = 1;
 constexpr int kErrRange = 2;    // |U| beyond the exact range of rint_magic
+constexpr int kErrLayout = 3;   // dynamic shared memory not 1024-byte aligned
 
 constexpr int TC_MAX_CLUSTER = 8;
 
@@ -707,7 +712,9 @@ struct StageRing {
     }
   }
 };
-static_assert((TC_NREC & (TC_NREC - 1)) == 0, "the record ring is indexed by masks");
+static_assert((TcForm<0>::NREC & (TcForm<0>::NREC - 1)) == 0 &&
+                  (TcForm<1>::NREC & (TcForm<1>::NREC - 1)) == 0,
+              "the record ring is indexed by masks");
 
 // The next item of this CTA (or cluster), or -1 when the launch's items are
 // all taken (see TcParams::claim).
@@ -807,14 +814,21 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
   constexpr int TILES = TcForm<kForm>::TILES;   // tiles per slot per stage
   constexpr int REC = KS * 32;                  // record bytes per stage
   constexpr int FLUSH = TC_FLUSH_SOURCES / KS;  // stages per accumulator flush
+  constexpr int TC_NREC = TcForm<kForm>::NREC;  // record stages
   // generator warps per stage in cluster mode (compile-time there; launches
   // without clusters take theirs from the parameters)
   constexpr int CL_TEAM = TcLayout<kForm>::TEAM;
-  extern __shared__ uint8_t smem_raw[];
-  // 1024-byte aligned base, formed by adding to the shared array (not by
-  // integer casts) so that every pointer derived from it stays a shared
-  // pointer and its loads are shared-memory loads, not generic ones
-  uint8_t* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  // The operand tiles need a 1024-byte aligned base (the 128-byte swizzle
+  // atoms); the launch reserves no slack for aligning it, which keeps the
+  // request within a smaller shared-memory carve-out.  A base that is not
+  // aligned is reported (HV_ERR_UNSUPPORTED on the host) before any shared
+  // memory is touched -- every CTA sees the same offset and returns.
+  if ((smem_u32(smem_raw) & 1023u) != 0u) {
+    if (threadIdx.x == 0) atomicExch(p.err, kErrLayout);
+    return;
+  }
+  uint8_t* smem = smem_raw;
   const int NS = p.nstages;
   const uint32_t op_base = smem_u32(smem);
   // a stage: the FP16 / split-BF16 tiles of every slot side by side, then
@@ -1014,8 +1028,15 @@ tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant
           const int s = (int)ring.s;
           const uint32_t par = ring.ph;
           const int rs = (int)(my_gs & (TC_NREC - 1));
-          if (!wait_warp(rec_full(rs), (my_gs / TC_NREC) & 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
+          // A parity wait is exact only while the barrier's previous phase
+          // has completed.  For the stage barrier that holds because this
+          // team's previous stage passed it (teams <= stages).  For the
+          // record barrier it follows from this order: once stage gs is free
+          // the MMAs have consumed stage gs - NS, so the records of every
+          // stage up to gs - NS, gs - NREC among them (NREC >= NS), have
+          // landed -- even when a record copy is withheld (fault injection).
           if (!wait_warp<kCluster>(smem_empty(s), par ^ 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
+          if (!wait_warp(rec_full(rs), (my_gs / TC_NREC) & 1, abort_flag, p.err, p.wait_ns)) { ok = false; break; }
           const SrcRec32* recs = reinterpret_cast<const SrcRec32*>(rec_smem + (size_t)rs * REC);
           const uint32_t stage_op = op_base + (uint32_t)s * stage_bytes;
           // unit u (sources 8 u .. 8 u + 7 of the stage) of slot index i
@@ -1568,7 +1589,10 @@ cudaError_t launch_form(const TcSimDesc* sims, int nsims, const void* rec, long 
   p.stall = stall;
   p.team_warps = team_warps;
   const int per_stage = TILES * p.max_slots * TC_SLOT;
-  const int fixed = 1024 /*alignment*/ + TC_NREC * KS * 32 + 512 /*barriers, holder*/;
+  // records and the barrier block (barriers, item ring, TMEM holder: at most
+  // 8 (2 NREC + 3 NS + 3 + 2 RING + RING) + 8 = 472 bytes)
+  constexpr int TC_NREC = TcForm<kForm>::NREC;
+  const int fixed = TC_NREC * KS * 32 + 480;
   const int max_stages = std::min(TC_MAX_STAGES, (TC_SMEM_LIMIT - fixed) / per_stage);
   p.nstages = max_stages;
   if (sims[0].tune.stages > 0) p.nstages = std::min(p.nstages, sims[0].tune.stages);
@@ -1578,15 +1602,37 @@ cudaError_t launch_form(const TcSimDesc* sims, int nsims, const void* rec, long 
   // stages (each team's previous stage was released before it).  Small
   // teams of one-slot launches are widened, and a stage cap below the
   // number of teams raised, until that holds.
-  while (TC_GEN_WARPS / p.team_warps > p.nstages && p.team_warps < TC_TEAM_WARPS)
+  while ((TC_GEN_WARPS / p.team_warps > p.nstages || TC_GEN_WARPS / p.team_warps > TC_NREC) &&
+         p.team_warps < TC_TEAM_WARPS)
     p.team_warps *= 2;
   const int teams = std::max(TC_GEN_WARPS / p.team_warps, cluster ? TC_GEN_WARPS / TC_TEAM_WARPS : 1);
   p.nstages = std::min(max_stages, std::max(p.nstages, teams));
-  if (p.nstages < 2 || teams > p.nstages || TC_GEN_WARPS / p.team_warps > TC_NREC)
+  if (p.nstages < 2 || teams > p.nstages || TC_GEN_WARPS / p.team_warps > TC_NREC ||
+      p.nstages > TC_NREC)
     return cudaErrorInvalidConfiguration;
   const int smem = fixed + p.nstages * per_stage;
   e = tc_configure();
   if (e != cudaSuccess) return e;
+  // The SM's on-chip memory is split between shared memory and the L1 cache
+  // that serves the beam gathers in fixed sizes; ask for the smallest
+  // shared size that holds the launch (with the CTA's reserved 1 KB), so
+  // that the rest is L1.
+  {
+    int carve_kb = 228;
+    for (int kb : {100, 132, 164, 196, 228})
+      if (kb * 1024 >= smem + 1024) {
+        carve_kb = kb;
+        break;
+      }
+    const int pct = (carve_kb * 100 + 227) / 228;
+    for (const void* k : {reinterpret_cast<const void*>(tc_vis_kernel<false, false, kForm>),
+                          reinterpret_cast<const void*>(tc_vis_kernel<false, true, kForm>),
+                          reinterpret_cast<const void*>(tc_vis_kernel<true, false, kForm>),
+                          reinterpret_cast<const void*>(tc_vis_kernel<true, true, kForm>)}) {
+      e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+      if (e != cudaSuccess) return e;
+    }
+  }
   if (!cluster) {
     const long long grid = std::min<long long>(num_sms, items);
     if (table) tc_vis_kernel<false, true, kForm><<<(int)grid, TC_THREADS, smem, st>>>(map, p);
