@@ -380,11 +380,12 @@ def load_peaks():
 
 # DRAM bytes per unit of work (slice x source above the horizon) of one
 # fused-kernel launch, measured once with ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum of the cluster launch on 350 antennas x 1,048,576
-# sources x 16 channels x 4 LSTs, 2.285 GB over 31,354,782 units): the
-# bench cannot read DRAM counters itself, so the figure is carried here and
-# scaled by the units each timed launch processed.
-TC_DRAM_BYTES_PER_UNIT = {"tc": 72.885}
+# dram__bytes_write.sum of the launch on 350 antennas x 1,048,576 sources x
+# 16 channels x 4 LSTs, which under ncu computes all 33,517,808 units:
+# split BF16 2.358 GB, FP16 + FP8 2.564 GB): the bench cannot read DRAM
+# counters itself, so the figure is carried here and scaled by the units
+# each timed launch processed.
+TC_DRAM_BYTES_PER_UNIT = {"tc": 70.355, "tc_fp16": 76.489}
 
 
 def run_ours(args):
