@@ -37,11 +37,15 @@ struct SimPlan {
   hv_sim in;
   int Np, ngroups, max_slots, nchunk, chunk, rec_stride;
   long long rec_row0;
-  size_t o_freqs, o_beam, o_U, o_umax, o_counts, o_blk, o_kv, o_crd, o_I, o_partial, o_groups;
-  size_t h_freqs;    // offset of the frequencies in the pinned host block
-  size_t h_groups;   // offset of its group table in the pinned host block
+  size_t o_beam, o_U, o_umax, o_counts, o_blk, o_kv, o_crd, o_I, o_partial;
+  // offsets in the constant block (the same in the pinned host block and at
+  // the start of the device arena)
+  size_t c_freqs, c_groups;
   int cls;           // index of its cluster class
 };
+
+// Prefix tables of the table-driven batch launches, in PrepPre's order.
+constexpr int kPrepTables = 9;
 
 }  // namespace
 
@@ -52,8 +56,13 @@ struct hv_batch {
   std::vector<SimPlan> sims;
   std::vector<std::vector<int>> classes;   // simulation indices per class
   std::vector<int> class_nchunk_div;       // split-K divisor per class
-  void* arena = nullptr;                   // device
+  std::vector<int> class_stages;           // operand-stage cap per class (0: as many as fit)
+  void* arena = nullptr;                   // device: the constant block, then the work areas
   size_t arena_bytes = 0;
+  // constant block: group tables, frequencies, the PrepSim table and the
+  // prefix tables; written once per layout and copied to the arena's start
+  size_t const_bytes = 0, c_prep = 0, c_pre = 0;
+  hv::PrepTotals totals{};
   void* rec = nullptr;                     // device records of every simulation
   long long rec_rows = 0;
   void* table = nullptr;                   // device simulation tables, per class
@@ -103,11 +112,33 @@ void chunking(int nsrc, int div, int* chunk, int* nchunk) {
   *nchunk = hv::ceil_div(S, *chunk);
 }
 
-// Lay out every simulation in the arena (split-K depth from the class divisor).
+// Lay out every simulation in the arena (split-K depth from the class
+// divisor): the constant block first, then each simulation's work areas.
 void layout(hv_batch* b) {
-  size_t off = 0, hoff = 0;
+  const int n = (int)b->sims.size();
+  // constant block: group tables (one per antenna count), frequencies,
+  // PrepSim table, prefix tables
+  size_t c = 0;
+  std::map<int, size_t> groups_at;  // nant -> offset
+  for (auto& s : b->sims) {
+    auto it = groups_at.find(s.in.nant);
+    if (it == groups_at.end()) {
+      groups_at[s.in.nant] = c;
+      s.c_groups = c;
+      c += up256(hv::tc_group_table_bytes(s.in.nant));
+    } else {
+      s.c_groups = it->second;
+    }
+    s.c_freqs = c;
+    c += up256(sizeof(double) * s.in.nfreq);
+  }
+  b->c_prep = c;
+  c += up256(sizeof(hv::PrepSim) * (size_t)n);
+  b->c_pre = c;
+  c += up256(sizeof(long long) * (size_t)(n + 1) * kPrepTables);
+  b->const_bytes = c;
+  size_t off = c;
   long long rows = 0;
-  std::map<int, std::pair<size_t, size_t>> groups_at;  // nant -> (device, host) offsets
   for (auto& s : b->sims) {
     const hv_sim& in = s.in;
     const int T = in.ntimes, F = in.nfreq, S = in.nsrc, P = in.beam_px;
@@ -117,7 +148,6 @@ void layout(hv_batch* b) {
     s.rec_stride = rec_stride_of(S);
     s.rec_row0 = rows;
     rows += (long long)T * s.rec_stride;
-    s.o_freqs = off; off += up256(sizeof(double) * F);
     s.o_beam = off; off += up256(sizeof(float) * (size_t)F * P * P * s.Np);
     s.o_U = off; off += up256(sizeof(hv::Ucoef32) * (size_t)T * F * s.Np);
     s.o_umax = off; off += up256(sizeof(float) * (size_t)T * F);
@@ -128,27 +158,103 @@ void layout(hv_batch* b) {
     s.o_I = off; off += up256(sizeof(float) * (size_t)std::max(S, 1));
     s.o_partial = off;
     off += up256(sizeof(float) * (size_t)T * F * s.nchunk * 2 * s.Np * s.Np);
-    auto it = groups_at.find(in.nant);
-    if (it == groups_at.end()) {
-      const size_t gb = hv::tc_group_table_bytes(in.nant);
-      groups_at[in.nant] = {off, hoff};
-      s.o_groups = off;
-      s.h_groups = hoff;
-      off += up256(gb);
-      hoff += up256(gb);
-    } else {
-      s.o_groups = it->second.first;
-      s.h_groups = it->second.second;
-    }
-    s.h_freqs = hoff;
-    hoff += up256(sizeof(double) * F);
   }
   b->arena_bytes = off;
   b->rec_rows = rows;
-  b->h_groups = 0;
-  b->h_table = hoff;
-  // one simulation table per class (an empty class still takes one entry)
-  b->host_bytes = hoff + up256(hv::tc_sim_table_bytes((int)(b->sims.size() + b->classes.size())));
+  // host block: the constant block, then one fused-kernel simulation table
+  // per class (an empty class still takes one entry)
+  b->h_table = c;
+  b->host_bytes = c + up256(hv::tc_sim_table_bytes((int)(b->sims.size() + b->classes.size())));
+}
+
+// The constant block in the host block: group tables, frequencies, the
+// PrepSim table (device addresses in the arena) and the prefix tables; and
+// the totals of the table-driven launches.
+void fill_constants(hv_batch* b) {
+  using namespace hv;
+  char* H = static_cast<char*>(b->host);
+  char* A = static_cast<char*>(b->arena);
+  const int n = (int)b->sims.size();
+  PrepSim* ps = reinterpret_cast<PrepSim*>(H + b->c_prep);
+  long long* pre = reinterpret_cast<long long*>(H + b->c_pre);
+  long long* pbeam = pre, *pucoef = pre + (n + 1), *pslice = pre + 2 * (n + 1),
+             *pkey = pre + 3 * (n + 1), *ppair = pre + 4 * (n + 1), *ptile = pre + 5 * (n + 1),
+             *pprep = pre + 6 * (n + 1), *prel = pre + 7 * (n + 1), *pred = pre + 8 * (n + 1);
+  PrepTotals t{};
+  for (int i = 0; i < n; ++i) {
+    SimPlan& s = b->sims[i];
+    const hv_sim& in = s.in;
+    tc_fill_group_table(in.nant, H + s.c_groups);
+    std::memcpy(H + s.c_freqs, in.freqs, sizeof(double) * in.nfreq);
+    const int T = in.ntimes, F = in.nfreq, S = in.nsrc, P = in.beam_px;
+    PrepSim x{};
+    x.antpos = in.antpos;
+    x.eq2tops = in.eq2tops;
+    x.crd_eq = in.crd_eq;
+    x.I_sky = in.I_sky;
+    x.bm = in.bm_cubes;
+    x.freqs = reinterpret_cast<const double*>(A + s.c_freqs);
+    x.beamT = reinterpret_cast<float*>(A + s.o_beam);
+    x.U = A + s.o_U;
+    x.umax = reinterpret_cast<float*>(A + s.o_umax);
+    x.counts = reinterpret_cast<int*>(A + s.o_counts);
+    x.blk = reinterpret_cast<int*>(A + s.o_blk);
+    x.kv = reinterpret_cast<unsigned long long*>(A + s.o_kv);
+    x.crd_s = reinterpret_cast<float*>(A + s.o_crd);
+    x.I_s = reinterpret_cast<float*>(A + s.o_I);
+    x.rec = static_cast<SrcRec32*>(b->rec) + s.rec_row0;
+    x.partial = reinterpret_cast<float*>(A + s.o_partial);
+    x.out = in.vis_out;
+    x.nant = in.nant;
+    x.Np = s.Np;
+    x.T = T;
+    x.F = F;
+    x.S = S;
+    x.P = P;
+    x.rec_stride = s.rec_stride;
+    x.chunk = s.chunk;
+    ps[i] = x;
+    // a simulation without times has nothing to prepare or reduce
+    const long long live = T > 0 ? 1 : 0;
+    const int nbt = ceil_div(in.nant, 32);
+    const long long key = (live && S > 0) ? sort_pad(S) : 0;
+    pbeam[i] = t.beam;   t.beam += live * (long long)ceil_div((long long)P * P, 32) * (s.Np / 32) * F;
+    pucoef[i] = t.ucoef; t.ucoef += (long long)T * F * s.Np;
+    pslice[i] = t.slice; t.slice += (long long)T * F;
+    pkey[i] = t.key;     t.key += key;
+    ppair[i] = t.pair;   t.pair += key / 2;
+    ptile[i] = t.tile;   t.tile += key / 2048;
+    pprep[i] = t.prep;   t.prep += (long long)prep_blocks(S) * T;
+    prel[i] = t.rel;     t.rel += (long long)ceil_div(s.rec_stride, 256) * T;
+    pred[i] = t.red;     t.red += (long long)nbt * (nbt + 1) / 2 * T * F;
+    t.max_key = std::max<long long>(t.max_key, key);
+  }
+  pbeam[n] = t.beam;
+  pucoef[n] = t.ucoef;
+  pslice[n] = t.slice;
+  pkey[n] = t.key;
+  ppair[n] = t.pair;
+  ptile[n] = t.tile;
+  pprep[n] = t.prep;
+  prel[n] = t.rel;
+  pred[n] = t.red;
+  b->totals = t;
+}
+
+hv::PrepPre device_pre(hv_batch* b) {
+  const int n = (int)b->sims.size();
+  const long long* pre = reinterpret_cast<const long long*>(static_cast<char*>(b->arena) + b->c_pre);
+  hv::PrepPre p{};
+  p.beam = pre;
+  p.ucoef = pre + (n + 1);
+  p.slice = pre + 2 * (n + 1);
+  p.key = pre + 3 * (n + 1);
+  p.pair = pre + 4 * (n + 1);
+  p.tile = pre + 5 * (n + 1);
+  p.prep = pre + 6 * (n + 1);
+  p.rel = pre + 7 * (n + 1);
+  p.red = pre + 8 * (n + 1);
+  return p;
 }
 
 // Device memory of the batch comes from the stream-ordered pool of the
@@ -177,62 +283,29 @@ int allocate(hv_batch* b) {
     b->host = hv_context_host_take(b->ctx, std::max<size_t>(b->host_bytes, 256), &b->host_cap);
     if (!b->host) return bfail(b, HV_ERR_OOM, "page-locked host block of %zu bytes", b->host_bytes);
   }
-  // constant host data: frequencies and group tables
-  char* h = static_cast<char*>(b->host);
-  for (auto& s : b->sims) {
-    hv::tc_fill_group_table(s.in.nant, h + s.h_groups);
-    std::memcpy(h + s.h_freqs, s.in.freqs, sizeof(double) * s.in.nfreq);
-  }
+  // the constant block, copied once per layout (it does not change between
+  // runs; the caller synchronises before the batch runs or is captured)
+  fill_constants(b);
+  HB_CK(cudaMemcpyAsync(b->arena, b->host, b->const_bytes, cudaMemcpyHostToDevice, st));
   return HV_OK;
 }
 
 // All work of the batch on stream st (no allocation, no synchronisation:
 // safe under stream capture).  timed_class >= 0: only the fused launch of
-// that class (for the autotuner).
+// that class (for the autotuner).  The preparation and the reduction of
+// every simulation are table-driven launches over the whole batch.
 int enqueue(hv_batch* b, cudaStream_t st, int timed_class = -1) {
   using namespace hv;
   char* A = static_cast<char*>(b->arena);
   char* H = static_cast<char*>(b->host);
   uint64_t nl = 0;
-  std::map<int, bool> groups_copied;
+  const PrepSim* sims = reinterpret_cast<const PrepSim*>(A + b->c_prep);
+  const PrepPre pre = device_pre(b);
+  const int n = (int)b->sims.size();
   if (timed_class < 0) {
-    for (auto& s : b->sims) {
-      const hv_sim& in = s.in;
-      const int T = in.ntimes, F = in.nfreq, S = in.nsrc, P = in.beam_px;
-      if (!groups_copied[in.nant]) {
-        groups_copied[in.nant] = true;
-        HB_CK(cudaMemcpyAsync(A + s.o_groups, H + s.h_groups, tc_group_table_bytes(in.nant),
-                              cudaMemcpyHostToDevice, st));
-      }
-      if (T == 0) continue;
-      HB_CK(cudaMemcpyAsync(A + s.o_freqs, H + s.h_freqs, sizeof(double) * F,
-                            cudaMemcpyHostToDevice, st));
-      float* beamT = reinterpret_cast<float*>(A + s.o_beam);
-      HB_CK(launch_beam_transpose<float>(in.bm_cubes, F, in.nant, P, s.Np, beamT, st));
-      HB_CK(launch_ucoef<float>(in.antpos, in.nant, s.Np, in.eq2tops, 0, T,
-                                reinterpret_cast<const double*>(A + s.o_freqs), F, A + s.o_U, st));
-      HB_CK(launch_ubound(A + s.o_U, T * F, s.Np, reinterpret_cast<float*>(A + s.o_umax), st));
-      nl += 3;
-      const float* crd = in.crd_eq;
-      const float* I = in.I_sky;
-      if (S > 0) {
-        int k = 0;
-        HB_CK(launch_sort_sources(in.crd_eq, in.I_sky, S, A + s.o_kv,
-                                  reinterpret_cast<float*>(A + s.o_crd),
-                                  reinterpret_cast<float*>(A + s.o_I), &k, st));
-        nl += k;
-        crd = reinterpret_cast<const float*>(A + s.o_crd);
-        I = reinterpret_cast<const float*>(A + s.o_I);
-      }
-      SrcRec32* rec = static_cast<SrcRec32*>(b->rec) + s.rec_row0;
-      HB_CK(launch_prep_strided<float>(crd, I, S, in.eq2tops, 0, T, P,
-                                       reinterpret_cast<int*>(A + s.o_blk), rec,
-                                       (size_t)s.rec_stride,
-                                       reinterpret_cast<int*>(A + s.o_counts), st));
-      HB_CK(launch_tc_relative(rec, (size_t)s.rec_stride, reinterpret_cast<int*>(A + s.o_counts),
-                               T, S, st));
-      nl += 3;
-    }
+    int k = 0;
+    HB_CK(launch_prepare_batch(sims, n, pre, b->totals, &k, st));
+    nl += k;
   }
   // one persistent fused launch per class; its CTAs claim the items in
   // table order, so the simulations with the largest items go first and the
@@ -254,7 +327,7 @@ int enqueue(hv_batch* b, cudaStream_t st, int timed_class = -1) {
       x.beamT = reinterpret_cast<const float*>(A + s.o_beam);
       x.umax = reinterpret_cast<const float*>(A + s.o_umax);
       x.partial = reinterpret_cast<float*>(A + s.o_partial);
-      x.groups = A + s.o_groups;
+      x.groups = A + s.c_groups;
       x.ngroups = s.ngroups;
       x.max_slots = s.max_slots;
       x.rec_row0 = s.rec_row0;
@@ -266,6 +339,7 @@ int enqueue(hv_batch* b, cudaStream_t st, int timed_class = -1) {
       x.P = s.in.beam_px;
       x.nsrc = s.in.nsrc;
       x.chunk = s.chunk;
+      x.tune.stages = b->class_stages.empty() ? 0 : b->class_stages[c];
       d.push_back(x);
     }
     if (!d.empty() && (timed_class < 0 || timed_class == (int)c)) {
@@ -280,7 +354,7 @@ int enqueue(hv_batch* b, cudaStream_t st, int timed_class = -1) {
         HB_CK(cudaEventRecord(e0, st));
       }
       // a class of one simulation in cluster mode shares its launch with the
-      // SMs no cluster fits on (not while timing split-K candidates)
+      // SMs no cluster fits on (not while timing candidates)
       TcShare* share = d.size() == 1 && timed_class < 0 ? hv_context_share(b->ctx) : nullptr;
       HB_CK(launch_tc_batch(d.data(), (int)d.size(), b->rec, b->rec_rows,
                             static_cast<char*>(b->table) + toff, H + b->h_table + toff, b->d_err,
@@ -296,15 +370,8 @@ int enqueue(hv_batch* b, cudaStream_t st, int timed_class = -1) {
     toff += tc_sim_table_bytes((int)d.size());
   }
   if (timed_class < 0) {
-    for (auto& s : b->sims) {
-      const hv_sim& in = s.in;
-      if (in.ntimes == 0) continue;
-      const size_t slice = (size_t)s.nchunk * 2 * s.Np * s.Np;
-      HB_CK(launch_reduce<float>(reinterpret_cast<float*>(A + s.o_partial), slice,
-                                 reinterpret_cast<const int*>(A + s.o_counts), in.ntimes,
-                                 in.nfreq, 0, in.ntimes, s.chunk, s.Np, in.nant, in.vis_out, st));
-      ++nl;
-    }
+    HB_CK(launch_reduce_batch(sims, n, pre, b->totals, st));
+    if (b->totals.red > 0) ++nl;
     b->launches_per_run = nl;
   }
   return HV_OK;
@@ -367,39 +434,50 @@ int hv_batch_create(hv_context* ctx, const hv_sim* sims, int nsims, unsigned fla
     cudaStream_t st = hv_context_stream(ctx);
     if (hv::tc_configure() != cudaSuccess) { r = HV_ERR_CUDA; break; }
     if (flags & HV_BATCH_AUTOTUNE) {
-      // split-K depth per class: time the fused launch with 1, 2 and 4
-      // chunks per slice on this batch and keep the fastest
-      r = enqueue(b, st);
-      if (r != HV_OK) break;
-      std::vector<int> best(b->classes.size(), 1);
-      for (size_t c = 0; c < b->classes.size() && r == HV_OK; ++c) {
-        float best_ms = 1e30f;
-        for (int div : {1, 2, 4}) {
-          b->class_nchunk_div[c] = div;
-          layout(b);
-          r = allocate(b);
-          if (r != HV_OK) break;
-          r = enqueue(b, st);  // preparation for this layout
-          if (r != HV_OK) break;
-          cudaEvent_t e0, e1;
-          cudaEventCreate(&e0);
-          cudaEventCreate(&e1);
-          cudaEventRecord(e0, st);
-          r = enqueue(b, st, (int)c);
-          cudaEventRecord(e1, st);
-          cudaEventSynchronize(e1);
-          float ms = 0.f;
-          cudaEventElapsedTime(&ms, e0, e1);
-          cudaEventDestroy(e0);
-          cudaEventDestroy(e1);
-          if (ms < best_ms) {
-            best_ms = ms;
-            best[c] = div;
-          }
-        }
-        b->class_nchunk_div[c] = best[c];
+      // per class: the split-K depth (divisor 1, 2 or 4 of the chunk count)
+      // and the cap on operand stages in shared memory (as many as fit, 5 or
+      // 3: fewer leave more of the SM's memory to the L1 cache of the beam
+      // gathers), each candidate's fused launch timed on this batch (the
+      // second of two runs), the fastest kept
+      b->class_stages.assign(b->classes.size(), 0);
+      std::vector<int> best_div(b->classes.size(), 1), best_st(b->classes.size(), 0);
+      std::vector<float> best_ms(b->classes.size(), 1e30f);
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        r = HV_ERR_CUDA;
+        break;
       }
+      for (int div : {1, 2, 4}) {
+        b->class_nchunk_div.assign(b->classes.size(), div);
+        layout(b);
+        r = allocate(b);
+        if (r == HV_OK) r = enqueue(b, st);  // preparation for this layout
+        for (size_t c = 0; c < b->classes.size() && r == HV_OK; ++c) {
+          for (int stages : {0, 5, 3}) {
+            b->class_stages[c] = stages;
+            float ms = 0.f;
+            for (int rep = 0; rep < 2 && r == HV_OK; ++rep) {
+              cudaEventRecord(e0, st);
+              r = enqueue(b, st, (int)c);
+              cudaEventRecord(e1, st);
+              cudaEventSynchronize(e1);
+              cudaEventElapsedTime(&ms, e0, e1);
+            }
+            if (r == HV_OK && ms < best_ms[c]) {
+              best_ms[c] = ms;
+              best_div[c] = div;
+              best_st[c] = stages;
+            }
+          }
+          b->class_stages[c] = 0;
+        }
+        if (r != HV_OK) break;
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
       if (r != HV_OK) break;
+      b->class_nchunk_div = best_div;
+      b->class_stages = best_st;
       layout(b);
       r = allocate(b);
       if (r != HV_OK) break;

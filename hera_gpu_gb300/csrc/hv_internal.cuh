@@ -142,4 +142,17 @@ __host__ __device__ inline int ceil_div(long long a, long long b) {
   return (int)((a + b - 1) / b);
 }
 
+// Segment of flattened index x: the largest i < n with pre[i] <= x (pre:
+// n + 1 non-decreasing prefix sums starting at 0).
+__device__ __forceinline__ int find_segment(const long long* __restrict__ pre, int n,
+                                            long long x) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(pre + mid) <= x) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 }  // namespace hv

@@ -8,6 +8,64 @@
 
 namespace hv {
 
+// --- batches: table-driven preparation and reduction -------------------------
+// One simulation of a batch for the launches that prepare or reduce every
+// simulation of the batch at once (device pointers; the batch's arena).
+// Each such launch flattens the blocks (or elements) of all simulations into
+// one index range; `pre` of that launch holds the nsims + 1 prefix sums, and
+// a block finds its simulation by binary search.
+struct PrepSim {
+  const float* antpos;
+  const float* eq2tops;
+  const float* crd_eq;
+  const float* I_sky;
+  const float* bm;       // (F, nant, P, P)
+  const double* freqs;   // (F,) device
+  float* beamT;          // [F][P*P][Np]
+  void* U;               // Ucoef32 [T][F][Np]
+  float* umax;           // [T * F]
+  int* counts;           // [T]
+  int* blk;              // [T][prep_blocks(S)]
+  unsigned long long* kv;  // sort_pad(S) words of the spatial sort (S > 0)
+  float* crd_s;          // (3, S) in spatial order
+  float* I_s;            // (S,) in spatial order
+  void* rec;             // SrcRec32 rows of time 0 (rec_stride per time)
+  float* partial;        // [T * F][nchunk][2][Np][Np]
+  void* out;             // (F, T, nant, nant) complex64
+  int nant, Np, T, F, S, P, rec_stride, chunk;
+};
+// Prefix sums of the flattened index range of each batch launch (nsims + 1
+// entries each, device memory).
+struct PrepPre {
+  const long long* beam;   // transpose tiles (32 x 32) x frequencies
+  const long long* ucoef;  // elements T * F * Np
+  const long long* slice;  // slices T * F
+  const long long* key;    // sort keys: sort_pad(S) per simulation with sources, else 0
+  const long long* pair;   // compare-exchange pairs: key / 2
+  const long long* tile;   // shared-memory sort tiles: key / 2048
+  const long long* prep;   // prep blocks x times
+  const long long* rel;    // units of 256 records x times (tc_relative)
+  const long long* red;    // upper 32 x 32 output tiles x slices
+};
+struct PrepTotals {
+  long long beam, ucoef, slice, key, pair, tile, prep, rel, red;
+  int max_key;             // the largest sort_pad(S) of the batch (0: no sources)
+};
+// The preparation of every simulation of a batch (spatial sort, beam
+// layout, phase coefficients and their bounds, records), table-driven: the
+// number of launches depends on the largest simulation's source count, not
+// on the number of simulations.  *launches is set to the kernels launched.
+cudaError_t launch_prepare_batch(const PrepSim* sims, int nsims, const PrepPre& pre,
+                                 const PrepTotals& tot, int* launches, cudaStream_t st);
+// The spatial sort of every simulation of a batch (hv_sort.cu): each one's
+// keys are sorted within its own segment, exactly as launch_sort_sources
+// sorts them alone.
+cudaError_t launch_sort_batch(const PrepSim* sims, int nsims, const PrepPre& pre,
+                              const PrepTotals& tot, int* launches, cudaStream_t st);
+// The split-K reduction of every simulation of a batch into its output.
+cudaError_t launch_reduce_batch(const PrepSim* sims, int nsims, const PrepPre& pre,
+                                const PrepTotals& tot, cudaStream_t st);
+
 // --- hv_prep.cu ------------------------------------------------------------
 // bm (nfreq, nant, P, P) -> beamT (nfreq, P*P, Np), zero for padded antennas.
 template <typename R>

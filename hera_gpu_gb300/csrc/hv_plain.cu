@@ -178,17 +178,20 @@ template <typename R> struct Acc;
 template <> struct Acc<float> { using type = KahanF; };
 template <> struct Acc<double> { using type = SumD; };
 
+// Upper 32 x 32 output tile `tile` of slice sl (block of 256 threads).
 template <typename R>
-__global__ void __launch_bounds__(256)
-reduce_kernel(const R* __restrict__ partial_base, size_t slice_stride,
-              const int* __restrict__ counts, int nf, int t0, int ntimes_out, int chunk, int Np,
-              int nant, typename Traits<R>::C* __restrict__ out_base) {
+__device__ __forceinline__ void reduce_tile(const R* __restrict__ partial_base,
+                                            size_t slice_stride, const int* __restrict__ counts,
+                                            int nf, int t0, int ntimes_out, int chunk, int Np,
+                                            int nant,
+                                            typename Traits<R>::C* __restrict__ out_base,
+                                            int tile, int sl,
+                                            typename Traits<R>::C (*T)[33]) {
   using C = typename Traits<R>::C;
-  __shared__ C T[32][33];
   const int nbt = ceil_div(nant, 32);
   int A, B;
-  decode_upper(blockIdx.x, nbt, A, B);
-  const int sl = blockIdx.y, tl = sl / nf, f = sl % nf;
+  decode_upper(tile, nbt, A, B);
+  const int tl = sl / nf, f = sl % nf;
   const R* partial = partial_base + (size_t)sl * slice_stride;
   C* out = out_base + ((size_t)f * ntimes_out + t0 + tl) * (size_t)nant * nant;
   const int n = counts[tl];
@@ -234,6 +237,38 @@ reduce_kernel(const R* __restrict__ partial_base, size_t slice_stride,
       out[(size_t)b * nant + a] = val;
     }
   }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256)
+reduce_kernel(const R* __restrict__ partial_base, size_t slice_stride,
+              const int* __restrict__ counts, int nf, int t0, int ntimes_out, int chunk, int Np,
+              int nant, typename Traits<R>::C* __restrict__ out_base) {
+  __shared__ typename Traits<R>::C T[32][33];
+  reduce_tile<R>(partial_base, slice_stride, counts, nf, t0, ntimes_out, chunk, Np, nant,
+                 out_base, blockIdx.x, blockIdx.y, T);
+}
+
+// Every simulation of a batch: its split-K chunks reduced into its output.
+__global__ void __launch_bounds__(256)
+reduce_batch_kernel(const PrepSim* __restrict__ sims, int nsims,
+                    const long long* __restrict__ pre) {
+  __shared__ float2 T[32][33];
+  const int si = find_segment(pre, nsims, blockIdx.x);
+  const PrepSim& sm = sims[si];
+  const int nbt = ceil_div(sm.nant, 32);
+  const int tiles = nbt * (nbt + 1) / 2;
+  const int local = (int)(blockIdx.x - __ldg(pre + si));
+  const size_t slice = (size_t)ceil_div(sm.S > 0 ? sm.S : 1, sm.chunk) * 2 * sm.Np * sm.Np;
+  reduce_tile<float>(sm.partial, slice, sm.counts, sm.F, 0, sm.T, sm.chunk, sm.Np, sm.nant,
+                     static_cast<float2*>(sm.out), local % tiles, local / tiles, T);
+}
+
+cudaError_t launch_reduce_batch(const PrepSim* sims, int nsims, const PrepPre& pre,
+                                const PrepTotals& tot, cudaStream_t st) {
+  if (tot.red <= 0) return cudaSuccess;
+  reduce_batch_kernel<<<(unsigned)tot.red, 256, 0, st>>>(sims, nsims, pre.red);
+  return cudaGetLastError();
 }
 
 template <typename R>

@@ -22,12 +22,11 @@
 namespace hv {
 
 // ---------------------------------------------------------------- beam ----
+// One 32 x 32 (pixel, antenna) tile of frequency f (block 32 x 8 threads).
 template <typename R>
-__global__ void beam_transpose_kernel(const R* __restrict__ bm, int nant, int PP, int Np,
-                                      R* __restrict__ beamT) {
-  __shared__ R tile[32][33];
-  const int f = blockIdx.z;
-  const int pix0 = blockIdx.x * 32, a0 = blockIdx.y * 32;
+__device__ __forceinline__ void beam_transpose_tile(const R* __restrict__ bm, int nant, int PP,
+                                                    int Np, R* __restrict__ beamT, int f,
+                                                    int pix0, int a0, R (*tile)[33]) {
   const R* src = bm + (size_t)f * nant * PP;
   R* dst = beamT + (size_t)f * PP * Np;
   for (int j = threadIdx.y; j < 32; j += blockDim.y) {
@@ -39,6 +38,14 @@ __global__ void beam_transpose_kernel(const R* __restrict__ bm, int nant, int PP
     const int pix = pix0 + j, a = a0 + threadIdx.x;
     if (pix < PP && a < Np) dst[(size_t)pix * Np + a] = tile[threadIdx.x][j];
   }
+}
+
+template <typename R>
+__global__ void beam_transpose_kernel(const R* __restrict__ bm, int nant, int PP, int Np,
+                                      R* __restrict__ beamT) {
+  __shared__ R tile[32][33];
+  beam_transpose_tile<R>(bm, nant, PP, Np, beamT, blockIdx.z, blockIdx.x * 32, blockIdx.y * 32,
+                         tile);
 }
 
 template <typename R>
@@ -66,14 +73,13 @@ __device__ __forceinline__ void store_ucoef(Ucoef64* U, size_t i, const double u
   U[i] = c;
 }
 
+// Element i = (tt * nfreq + f) * Np + a of U.
 template <typename R>
-__global__ void ucoef_kernel(const R* __restrict__ antpos, int nant, int Np,
-                             const R* __restrict__ eq2tops, int t0, int nt,
-                             const double* __restrict__ freqs, int nfreq,
-                             typename Traits<R>::U* __restrict__ U) {
-  const size_t total = (size_t)nt * nfreq * Np;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
-       i += (size_t)gridDim.x * blockDim.x) {
+__device__ __forceinline__ void ucoef_element(const R* __restrict__ antpos, int nant, int Np,
+                                              const R* __restrict__ eq2tops, int t0,
+                                              const double* __restrict__ freqs, int nfreq,
+                                              typename Traits<R>::U* __restrict__ U, size_t i) {
+  {
     const int a = (int)(i % Np);
     const int f = (int)((i / Np) % nfreq);
     const int tt = (int)(i / ((size_t)Np * nfreq));
@@ -94,6 +100,17 @@ __global__ void ucoef_kernel(const R* __restrict__ antpos, int nant, int Np,
 }
 
 template <typename R>
+__global__ void ucoef_kernel(const R* __restrict__ antpos, int nant, int Np,
+                             const R* __restrict__ eq2tops, int t0, int nt,
+                             const double* __restrict__ freqs, int nfreq,
+                             typename Traits<R>::U* __restrict__ U) {
+  const size_t total = (size_t)nt * nfreq * Np;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x)
+    ucoef_element<R>(antpos, nant, Np, eq2tops, t0, freqs, nfreq, U, i);
+}
+
+template <typename R>
 cudaError_t launch_ucoef(const R* antpos, int nant, int Np, const R* eq2tops, int t0,
                          int nt, const double* d_freqs, int nfreq, void* U,
                          cudaStream_t st) {
@@ -105,10 +122,9 @@ cudaError_t launch_ucoef(const R* antpos, int nant, int Np, const R* eq2tops, in
   return cudaGetLastError();
 }
 
-__global__ void __launch_bounds__(256)
-ubound_kernel(const Ucoef32* __restrict__ U, int Np, float* __restrict__ umax) {
-  __shared__ float red[8];
-  const Ucoef32* u = U + (size_t)blockIdx.x * Np;
+// Bound of one slice (block of 256 threads).
+__device__ __forceinline__ void ubound_slice(const Ucoef32* __restrict__ u, int Np,
+                                             float* __restrict__ out, float* red) {
   float m = 0.f;
   for (int a = threadIdx.x; a < Np; a += blockDim.x) {
     const Ucoef32 c = u[a];
@@ -119,8 +135,14 @@ ubound_kernel(const Ucoef32* __restrict__ U, int Np, float* __restrict__ umax) {
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int w = 1; w < 8; ++w) m = fmaxf(m, red[w]);
-    umax[blockIdx.x] = m * 1.0001f;  // margin for the rounding of the sum
+    *out = m * 1.0001f;  // margin for the rounding of the sum
   }
+}
+
+__global__ void __launch_bounds__(256)
+ubound_kernel(const Ucoef32* __restrict__ U, int Np, float* __restrict__ umax) {
+  __shared__ float red[8];
+  ubound_slice(U + (size_t)blockIdx.x * Np, Np, umax + blockIdx.x, red);
 }
 
 cudaError_t launch_ubound(const void* U, int nslices, int Np, float* umax, cudaStream_t st) {
@@ -129,7 +151,8 @@ cudaError_t launch_ubound(const void* U, int nslices, int Np, float* umax, cudaS
 }
 
 // -------------------------------------------------------- source prep ----
-int prep_blocks(int nsrc) { return nsrc > 0 ? ceil_div(nsrc, kPrepBlock) : 1; }
+__host__ __device__ int prep_blocks_of(int nsrc) { return nsrc > 0 ? ceil_div(nsrc, kPrepBlock) : 1; }
+int prep_blocks(int nsrc) { return prep_blocks_of(nsrc); }
 
 template <typename R>
 __device__ __forceinline__ void load_rot(const R* __restrict__ eq2tops, int t, double* rot) {
@@ -141,16 +164,16 @@ __device__ __forceinline__ double top_z(const double* rot, double x, double y, d
   return fma(rot[6], x, fma(rot[7], y, rot[8] * z));
 }
 
+// Source block bx of time tt: sources above the horizon, into
+// block_counts[tt * nblk + bx].
 template <typename R>
-__global__ void __launch_bounds__(kPrepBlock)
-prep_count_kernel(const R* __restrict__ crd_eq, int nsrc, const R* __restrict__ eq2tops,
-                  int t0, int nblk, int* __restrict__ block_counts) {
-  __shared__ double rot[9];
-  __shared__ int warp_cnt[kPrepBlock / 32];
-  const int tt = blockIdx.y;
+__device__ __forceinline__ void prep_count_block(const R* __restrict__ crd_eq, int nsrc,
+                                                 const R* __restrict__ eq2tops, int t0, int nblk,
+                                                 int* __restrict__ block_counts, int bx, int tt,
+                                                 double* rot, int* warp_cnt) {
   load_rot(eq2tops, t0 + tt, rot);
   __syncthreads();
-  const int s = blockIdx.x * kPrepBlock + threadIdx.x;
+  const int s = bx * kPrepBlock + threadIdx.x;
   bool up = false;
   if (s < nsrc)
     up = top_z(rot, crd_eq[s], crd_eq[(size_t)nsrc + s], crd_eq[2 * (size_t)nsrc + s]) > 0.0;
@@ -160,8 +183,18 @@ prep_count_kernel(const R* __restrict__ crd_eq, int nsrc, const R* __restrict__ 
   if (threadIdx.x < 32) {
     int c = warp_cnt[threadIdx.x];
     for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-    if (threadIdx.x == 0) block_counts[(size_t)tt * nblk + blockIdx.x] = c;
+    if (threadIdx.x == 0) block_counts[(size_t)tt * nblk + bx] = c;
   }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kPrepBlock)
+prep_count_kernel(const R* __restrict__ crd_eq, int nsrc, const R* __restrict__ eq2tops,
+                  int t0, int nblk, int* __restrict__ block_counts) {
+  __shared__ double rot[9];
+  __shared__ int warp_cnt[kPrepBlock / 32];
+  prep_count_block<R>(crd_eq, nsrc, eq2tops, t0, nblk, block_counts, blockIdx.x, blockIdx.y, rot,
+                      warp_cnt);
 }
 
 __device__ __forceinline__ void fill_rec(SrcRec32& r, double x, double y, double z,
@@ -189,22 +222,32 @@ __device__ __forceinline__ int beam_axis(double c, int P, double& w) {
   return (int)fmin(fmax(fb, 0.0), (double)(P - 2));
 }
 
+// Source block bx of time tt: records of its sources above the horizon at
+// their place in catalogue order (after the blocks before it).
+struct PrepWriteSmem {
+  double rot[9];
+  int warp_cnt[kPrepBlock / 32];
+  int red[kPrepBlock / 32];
+  int base;
+};
 template <typename R>
-__global__ void __launch_bounds__(kPrepBlock)
-prep_write_kernel(const R* __restrict__ crd_eq, const R* __restrict__ I_sky, int nsrc,
-                  size_t rec_stride, const R* __restrict__ eq2tops, int t0, int nblk, int P,
-                  const int* __restrict__ block_counts,
-                  typename Traits<R>::Rec* __restrict__ rec, int* __restrict__ count) {
-  __shared__ double rot[9];
-  __shared__ int warp_cnt[kPrepBlock / 32];
-  __shared__ int red[kPrepBlock / 32];
-  __shared__ int base;
-  const int tt = blockIdx.y;
+__device__ __forceinline__ void prep_write_block(const R* __restrict__ crd_eq,
+                                                 const R* __restrict__ I_sky, int nsrc,
+                                                 size_t rec_stride, const R* __restrict__ eq2tops,
+                                                 int t0, int nblk, int P,
+                                                 const int* __restrict__ block_counts,
+                                                 typename Traits<R>::Rec* __restrict__ rec,
+                                                 int* __restrict__ count, int bx, int tt,
+                                                 PrepWriteSmem& sm) {
+  double* rot = sm.rot;
+  int* warp_cnt = sm.warp_cnt;
+  int* red = sm.red;
+  int& base = sm.base;
   const int* bc = block_counts + (size_t)tt * nblk;
   load_rot(eq2tops, t0 + tt, rot);
   // offset of this block = sum of the counts of the blocks before it
   int part = 0;
-  for (int i = threadIdx.x; i < (int)blockIdx.x; i += kPrepBlock) part += bc[i];
+  for (int i = threadIdx.x; i < bx; i += kPrepBlock) part += bc[i];
   for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
   __syncthreads();
@@ -213,7 +256,7 @@ prep_write_kernel(const R* __restrict__ crd_eq, const R* __restrict__ I_sky, int
     for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
     if (threadIdx.x == 0) base = c;
   }
-  const int s = blockIdx.x * kPrepBlock + threadIdx.x;
+  const int s = bx * kPrepBlock + threadIdx.x;
   double x = 0, y = 0, z = 0, tx = 0, ty = 0, tz = 0;
   bool up = false;
   __syncthreads();
@@ -236,7 +279,7 @@ prep_write_kernel(const R* __restrict__ crd_eq, const R* __restrict__ I_sky, int
       if (lane >= o) incl += n;
     }
     red[lane] = incl - c;
-    if (blockIdx.x == nblk - 1 && lane == 31) count[tt] = base + incl;
+    if (bx == nblk - 1 && lane == 31) count[tt] = base + incl;
   }
   __syncthreads();
   if (up) {
@@ -248,6 +291,17 @@ prep_write_kernel(const R* __restrict__ crd_eq, const R* __restrict__ I_sky, int
     fill_rec(r, x, y, z, sqrt((double)I_sky[s]), py * P + px, fx, fy);
     rec[(size_t)tt * rec_stride + idx] = r;
   }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kPrepBlock)
+prep_write_kernel(const R* __restrict__ crd_eq, const R* __restrict__ I_sky, int nsrc,
+                  size_t rec_stride, const R* __restrict__ eq2tops, int t0, int nblk, int P,
+                  const int* __restrict__ block_counts,
+                  typename Traits<R>::Rec* __restrict__ rec, int* __restrict__ count) {
+  __shared__ PrepWriteSmem sm;
+  prep_write_block<R>(crd_eq, I_sky, nsrc, rec_stride, eq2tops, t0, nblk, P, block_counts, rec,
+                      count, blockIdx.x, blockIdx.y, sm);
 }
 
 template <typename R>
@@ -284,14 +338,14 @@ cudaError_t launch_prep(const R* crd_eq, const R* I_sky, int nsrc, const R* eq2t
 //    slice at hand, and loads the four beam corners once for such a unit;
 //  * records [count, round_up(count, 32)) are zeroed, so a partial last stage
 //    reads sources of zero amplitude at beam pixel 0.
-__global__ void __launch_bounds__(256)
-tc_relative_kernel(SrcRec32* __restrict__ rec, size_t rec_stride,
-                   const int* __restrict__ counts) {
-  const int tt = blockIdx.y;
+// Records [i0, i0 + 256) of time tt (block of 256 threads).
+__device__ __forceinline__ void tc_relative_span(SrcRec32* __restrict__ rec, size_t rec_stride,
+                                                 const int* __restrict__ counts, int tt, int i0) {
   SrcRec32* r = rec + (size_t)tt * rec_stride;
   const int n = counts[tt];
   const int npad = (n + 31) & ~31;
-  for (int i0 = blockIdx.x * blockDim.x; i0 < npad; i0 += gridDim.x * blockDim.x) {
+  if (i0 >= npad) return;
+  {
     const int i = i0 + threadIdx.x;  // a warp covers 4 whole units
     float d1 = 0.f;
     int pix = -1, ref_pix = -1;
@@ -316,6 +370,15 @@ tc_relative_kernel(SrcRec32* __restrict__ rec, size_t rec_stride,
       r[i] = SrcRec32{};
     }
   }
+}
+
+__global__ void __launch_bounds__(256)
+tc_relative_kernel(SrcRec32* __restrict__ rec, size_t rec_stride,
+                   const int* __restrict__ counts) {
+  const int tt = blockIdx.y;
+  const int npad = (counts[tt] + 31) & ~31;
+  for (int i0 = blockIdx.x * blockDim.x; i0 < npad; i0 += gridDim.x * blockDim.x)
+    tc_relative_span(rec, rec_stride, counts, tt, i0);
 }
 
 cudaError_t launch_tc_relative(void* rec, size_t rec_stride, const int* counts, int nt, int nsrc,
@@ -410,6 +473,132 @@ cudaError_t launch_slice_bound(const void* rec, size_t rec_stride, const int* co
                                            pixmax, nf, P * P, P > 1 ? 1 : 0, P > 1 ? P : 0,
                                            reinterpret_cast<unsigned*>(sbound));
   return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ batches ----
+// The same preparation for every simulation of a batch in one launch per
+// step; a block finds its simulation in the step's prefix table.
+__global__ void __launch_bounds__(256)
+beam_transpose_batch_kernel(const PrepSim* __restrict__ sims, int nsims,
+                            const long long* __restrict__ pre) {
+  __shared__ float tile[32][33];
+  const long long b = blockIdx.x;
+  const int si = find_segment(pre, nsims, b);
+  const PrepSim& sm = sims[si];
+  const int PP = sm.P * sm.P;
+  const int tx = ceil_div(PP, 32), ty = sm.Np / 32;
+  const long long local = b - __ldg(pre + si);
+  const int f = (int)(local / ((long long)tx * ty));
+  const int rem = (int)(local % ((long long)tx * ty));
+  beam_transpose_tile<float>(sm.bm, sm.nant, PP, sm.Np, sm.beamT, f, (rem % tx) * 32,
+                             (rem / tx) * 32, tile);
+}
+
+__global__ void __launch_bounds__(256)
+ucoef_batch_kernel(const PrepSim* __restrict__ sims, int nsims, const long long* __restrict__ pre,
+                   long long total) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int si = find_segment(pre, nsims, e);
+    const PrepSim& sm = sims[si];
+    ucoef_element<float>(sm.antpos, sm.nant, sm.Np, sm.eq2tops, 0, sm.freqs, sm.F,
+                         static_cast<Ucoef32*>(sm.U), (size_t)(e - __ldg(pre + si)));
+  }
+}
+
+__global__ void __launch_bounds__(256)
+ubound_batch_kernel(const PrepSim* __restrict__ sims, int nsims,
+                    const long long* __restrict__ pre) {
+  __shared__ float red[8];
+  const int si = find_segment(pre, nsims, blockIdx.x);
+  const PrepSim& sm = sims[si];
+  const long long l = blockIdx.x - __ldg(pre + si);
+  ubound_slice(static_cast<const Ucoef32*>(sm.U) + l * sm.Np, sm.Np, sm.umax + l, red);
+}
+
+// the catalogue a simulation's records are made from: the spatially sorted
+// copy, or the input when it has no sources
+__device__ __forceinline__ void batch_catalogue(const PrepSim& sm, const float*& crd,
+                                                const float*& I) {
+  crd = sm.S > 0 ? sm.crd_s : sm.crd_eq;
+  I = sm.S > 0 ? sm.I_s : sm.I_sky;
+}
+
+__global__ void __launch_bounds__(kPrepBlock)
+prep_count_batch_kernel(const PrepSim* __restrict__ sims, int nsims,
+                        const long long* __restrict__ pre) {
+  __shared__ double rot[9];
+  __shared__ int warp_cnt[kPrepBlock / 32];
+  const int si = find_segment(pre, nsims, blockIdx.x);
+  const PrepSim& sm = sims[si];
+  const int nblk = prep_blocks_of(sm.S);
+  const int local = (int)(blockIdx.x - __ldg(pre + si));
+  const float *crd, *I;
+  batch_catalogue(sm, crd, I);
+  prep_count_block<float>(crd, sm.S, sm.eq2tops, 0, nblk, sm.blk, local % nblk, local / nblk,
+                          rot, warp_cnt);
+}
+
+__global__ void __launch_bounds__(kPrepBlock)
+prep_write_batch_kernel(const PrepSim* __restrict__ sims, int nsims,
+                        const long long* __restrict__ pre) {
+  __shared__ PrepWriteSmem smw;
+  const int si = find_segment(pre, nsims, blockIdx.x);
+  const PrepSim& sm = sims[si];
+  const int nblk = prep_blocks_of(sm.S);
+  const int local = (int)(blockIdx.x - __ldg(pre + si));
+  const float *crd, *I;
+  batch_catalogue(sm, crd, I);
+  prep_write_block<float>(crd, I, sm.S, (size_t)sm.rec_stride, sm.eq2tops, 0, nblk, sm.P, sm.blk,
+                          static_cast<SrcRec32*>(sm.rec), sm.counts, local % nblk, local / nblk,
+                          smw);
+}
+
+__global__ void __launch_bounds__(256)
+tc_relative_batch_kernel(const PrepSim* __restrict__ sims, int nsims,
+                         const long long* __restrict__ pre) {
+  const int si = find_segment(pre, nsims, blockIdx.x);
+  const PrepSim& sm = sims[si];
+  const int nb = ceil_div(sm.rec_stride, 256);
+  const int local = (int)(blockIdx.x - __ldg(pre + si));
+  tc_relative_span(static_cast<SrcRec32*>(sm.rec), (size_t)sm.rec_stride, sm.counts, local / nb,
+                   (local % nb) * 256);
+}
+
+cudaError_t launch_prepare_batch(const PrepSim* sims, int nsims, const PrepPre& pre,
+                                 const PrepTotals& tot, int* launches, cudaStream_t st) {
+  int nl = 0;
+  cudaError_t e;
+#define HV_PB(launch)                                 \
+  do {                                                \
+    launch;                                           \
+    if ((e = cudaGetLastError()) != cudaSuccess) return e; \
+    ++nl;                                             \
+  } while (0)
+  if (tot.beam > 0)
+    HV_PB((beam_transpose_batch_kernel<<<(unsigned)tot.beam, dim3(32, 8), 0, st>>>(sims, nsims,
+                                                                                    pre.beam)));
+  if (tot.ucoef > 0)
+    HV_PB((ucoef_batch_kernel<<<(unsigned)std::min<long long>((tot.ucoef + 255) / 256, 152 * 32),
+                                 256, 0, st>>>(sims, nsims, pre.ucoef, tot.ucoef)));
+  if (tot.slice > 0)
+    HV_PB((ubound_batch_kernel<<<(unsigned)tot.slice, 256, 0, st>>>(sims, nsims, pre.slice)));
+  if (tot.key > 0) {
+    int k = 0;
+    if ((e = launch_sort_batch(sims, nsims, pre, tot, &k, st)) != cudaSuccess) return e;
+    nl += k;
+  }
+  if (tot.prep > 0) {
+    HV_PB((prep_count_batch_kernel<<<(unsigned)tot.prep, kPrepBlock, 0, st>>>(sims, nsims,
+                                                                              pre.prep)));
+    HV_PB((prep_write_batch_kernel<<<(unsigned)tot.prep, kPrepBlock, 0, st>>>(sims, nsims,
+                                                                              pre.prep)));
+  }
+  if (tot.rel > 0)
+    HV_PB((tc_relative_batch_kernel<<<(unsigned)tot.rel, 256, 0, st>>>(sims, nsims, pre.rel)));
+#undef HV_PB
+  if (launches) *launches = nl;
+  return cudaSuccess;
 }
 
 template cudaError_t launch_beam_transpose<float>(const float*, int, int, int, int, float*, cudaStream_t);

@@ -25,10 +25,11 @@ __device__ __forceinline__ uint32_t spread16(uint32_t a) {
   return a;
 }
 
-__global__ void sort_keys_kernel(const float* __restrict__ crd_eq, int nsrc, int npad,
-                                 unsigned long long* __restrict__ kv) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npad; i += gridDim.x * blockDim.x) {
-    unsigned long long v = ~0ull;
+// Sort word of source i: (Morton key << 32) | i, or all ones for padding.
+__device__ __forceinline__ unsigned long long sort_word(const float* __restrict__ crd_eq,
+                                                        int nsrc, int i) {
+  unsigned long long v = ~0ull;
+  {
     if (i < nsrc) {
       const float x = crd_eq[i], y = crd_eq[(size_t)nsrc + i], z = crd_eq[2 * (size_t)nsrc + i];
       const float n = fabsf(x) + fabsf(y) + fabsf(z);
@@ -45,8 +46,14 @@ __global__ void sort_keys_kernel(const float* __restrict__ crd_eq, int nsrc, int
       const uint32_t key = spread16((uint32_t)qu) | (spread16((uint32_t)qw) << 1);
       v = ((unsigned long long)key << 32) | (uint32_t)i;
     }
-    kv[i] = v;
   }
+  return v;
+}
+
+__global__ void sort_keys_kernel(const float* __restrict__ crd_eq, int nsrc, int npad,
+                                 unsigned long long* __restrict__ kv) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npad; i += gridDim.x * blockDim.x)
+    kv[i] = sort_word(crd_eq, nsrc, i);
 }
 
 // One compare-exchange pass of the bitonic network (stride j, sequence k).
@@ -103,6 +110,115 @@ __global__ void gather_sorted_kernel(const float* __restrict__ crd_eq, const flo
     crd_s[2 * (size_t)nsrc + i] = crd_eq[2 * (size_t)nsrc + src];
     I_s[i] = I[src];
   }
+}
+
+// ------------------------------------------------------------ batches ----
+// Every simulation of a batch sorted in one set of launches: simulation s
+// owns a segment of sort_pad(S_s) words (its own kv buffer), and each pass
+// of the network runs within every segment long enough for it, so a
+// simulation's order is exactly the one launch_sort_sources gives it alone.
+__global__ void sort_keys_batch_kernel(const PrepSim* __restrict__ sims, int nsims,
+                                       const long long* __restrict__ pre, long long total) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int si = find_segment(pre, nsims, e);
+    const PrepSim& sm = sims[si];
+    const int l = (int)(e - __ldg(pre + si));
+    sm.kv[l] = sort_word(sm.crd_eq, sm.S, l);
+  }
+}
+
+__global__ void bitonic_global_batch_kernel(const PrepSim* __restrict__ sims, int nsims,
+                                            const long long* __restrict__ pre, long long total,
+                                            int j, int k) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int si = find_segment(pre, nsims, e);
+    const long long n = 2 * (__ldg(pre + si + 1) - __ldg(pre + si));
+    if ((long long)k > n) continue;  // this segment is sorted already
+    unsigned long long* kv = sims[si].kv;
+    const int i = (int)(e - __ldg(pre + si));
+    const int lo = ((i / j) * 2 * j) + (i % j);
+    const int hi = lo + j;
+    const bool up = (lo & k) == 0;
+    const unsigned long long a = kv[lo], b = kv[hi];
+    if ((a > b) == up) {
+      kv[lo] = b;
+      kv[hi] = a;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(1024)
+bitonic_shared_batch_kernel(const PrepSim* __restrict__ sims, int nsims,
+                            const long long* __restrict__ pre, int k0, int k1) {
+  __shared__ unsigned long long s[kSortTile];
+  const int si = find_segment(pre, nsims, blockIdx.x);
+  const long long n = (long long)kSortTile * (__ldg(pre + si + 1) - __ldg(pre + si));
+  if ((long long)k0 > n) return;  // the whole block: one segment
+  unsigned long long* kv = sims[si].kv;
+  const size_t base = (size_t)(blockIdx.x - __ldg(pre + si)) * kSortTile;
+  s[threadIdx.x] = kv[base + threadIdx.x];
+  s[threadIdx.x + 1024] = kv[base + threadIdx.x + 1024];
+  __syncthreads();
+  const int kmax = (int)min((long long)k1, n);
+  for (int k = k0; k <= kmax; k <<= 1) {
+    for (int j = min(k / 2, kSortTile / 2); j > 0; j >>= 1) {
+      const int t = threadIdx.x;
+      const int lo = ((t / j) * 2 * j) + (t % j);
+      const int hi = lo + j;
+      const bool up = ((base + lo) & (size_t)k) == 0;
+      const unsigned long long a = s[lo], b = s[hi];
+      if ((a > b) == up) {
+        s[lo] = b;
+        s[hi] = a;
+      }
+      __syncthreads();
+    }
+  }
+  kv[base + threadIdx.x] = s[threadIdx.x];
+  kv[base + threadIdx.x + 1024] = s[threadIdx.x + 1024];
+}
+
+__global__ void gather_sorted_batch_kernel(const PrepSim* __restrict__ sims, int nsims,
+                                           const long long* __restrict__ pre, long long total) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int si = find_segment(pre, nsims, e);
+    const PrepSim& sm = sims[si];
+    const int i = (int)(e - __ldg(pre + si));
+    if (i >= sm.S) continue;
+    const uint32_t src = (uint32_t)(sm.kv[i] & 0xffffffffu);
+    const size_t S = (size_t)sm.S;
+    sm.crd_s[i] = sm.crd_eq[src];
+    sm.crd_s[S + i] = sm.crd_eq[S + src];
+    sm.crd_s[2 * S + i] = sm.crd_eq[2 * S + src];
+    sm.I_s[i] = sm.I_sky[src];
+  }
+}
+
+cudaError_t launch_sort_batch(const PrepSim* sims, int nsims, const PrepPre& pre,
+                              const PrepTotals& tot, int* launches, cudaStream_t st) {
+  int nl = 0;
+  const int gk = (int)std::min<long long>((tot.key + 255) / 256, 152 * 16);
+  const int gp = (int)std::min<long long>((tot.pair + 255) / 256, 152 * 16);
+  sort_keys_batch_kernel<<<gk, 256, 0, st>>>(sims, nsims, pre.key, tot.key);
+  ++nl;
+  bitonic_shared_batch_kernel<<<(unsigned)tot.tile, 1024, 0, st>>>(sims, nsims, pre.tile, 2,
+                                                                    kSortTile);
+  ++nl;
+  for (int k = 2 * kSortTile; k <= tot.max_key; k <<= 1) {
+    for (int j = k / 2; j >= kSortTile; j >>= 1) {
+      bitonic_global_batch_kernel<<<gp, 256, 0, st>>>(sims, nsims, pre.pair, tot.pair, j, k);
+      ++nl;
+    }
+    bitonic_shared_batch_kernel<<<(unsigned)tot.tile, 1024, 0, st>>>(sims, nsims, pre.tile, k, k);
+    ++nl;
+  }
+  gather_sorted_batch_kernel<<<gk, 256, 0, st>>>(sims, nsims, pre.key, tot.key);
+  ++nl;
+  if (launches) *launches = nl;
+  return cudaGetLastError();
 }
 
 int sort_pad(int nsrc) {
