@@ -116,6 +116,19 @@ herk_plain_kernel(const typename Traits<R>::C* __restrict__ v, const int* __rest
     }
     __syncthreads();
     if (s + kHK < s1) gload(s + kHK);
+    // FP32: each stage's 16 sources are summed from zero and the stage sum
+    // is added to the running total, so the total's rounding walks over
+    // kPlainChunk / 16 additions instead of kPlainChunk (about 4x less
+    // error at the same chunk); FP64 sums straight into the total
+    constexpr bool kTwoLevel = sizeof(R) == 4;
+    R st_re[4][4], st_im[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        st_re[i][j] = kTwoLevel ? R(0) : acc_re[i][j];
+        st_im[i][j] = kTwoLevel ? R(0) : acc_im[i][j];
+      }
 #pragma unroll
     for (int k = 0; k < kHK; ++k) {
       C a[4], b[4];
@@ -128,10 +141,17 @@ herk_plain_kernel(const typename Traits<R>::C* __restrict__ v, const int* __rest
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           // v_a conj(v_b) = (ar br + ai bi) + i (ai br - ar bi)
-          acc_re[i][j] = fma(a[i].x, b[j].x, fma(a[i].y, b[j].y, acc_re[i][j]));
-          acc_im[i][j] = fma(a[i].y, b[j].x, fma(-a[i].x, b[j].y, acc_im[i][j]));
+          st_re[i][j] = fma(a[i].x, b[j].x, fma(a[i].y, b[j].y, st_re[i][j]));
+          st_im[i][j] = fma(a[i].y, b[j].x, fma(-a[i].x, b[j].y, st_im[i][j]));
         }
     }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        acc_re[i][j] = kTwoLevel ? acc_re[i][j] + st_re[i][j] : st_re[i][j];
+        acc_im[i][j] = kTwoLevel ? acc_im[i][j] + st_im[i][j] : st_im[i][j];
+      }
     __syncthreads();
   }
   R* pre = partial + (size_t)blockIdx.y * 2 * Np * Np;
