@@ -155,13 +155,58 @@ __host__ __device__ int prep_blocks_of(int nsrc) { return nsrc > 0 ? ceil_div(ns
 int prep_blocks(int nsrc) { return prep_blocks_of(nsrc); }
 
 template <typename R>
-__device__ __forceinline__ void load_rot(const R* __restrict__ eq2tops, int t, double* rot) {
-  if (threadIdx.x < 9) rot[threadIdx.x] = (double)eq2tops[(size_t)t * 9 + threadIdx.x];
+__device__ __forceinline__ void load_rot(const R* __restrict__ eq2tops, int t, R* rot) {
+  if (threadIdx.x < 9) rot[threadIdx.x] = eq2tops[(size_t)t * 9 + threadIdx.x];
 }
 
-// z component of eq2top . s (topocentric up), FP64.
-__device__ __forceinline__ double top_z(const double* rot, double x, double y, double z) {
-  return fma(rot[6], x, fma(rot[7], y, rot[8] * z));
+// Topocentric geometry of one source at one time: the horizon test on the
+// z component of eq2top . s, and the beam corner and weights from its x
+// and y components.
+//
+// FP32 inputs: each component is formed as an unevaluated sum hi + lo with
+// error-free transformations (TwoProduct by FMA, TwoSum; the compensated dot
+// product Dot2 of Ogita, Rump and Oishi, "Accurate sum and dot product",
+// SIAM J. Sci. Comput. 26(6), 2005), whose error is at most
+// u |r . s| + gamma_3^2 sum |r_i s_i| (u = 2^-24): the horizon test and the
+// weights come out as they would from an FP64 evaluation, in FP32
+// arithmetic (this part's FP64 rate is a small fraction of its FP32 rate,
+// and the work is per source and time).  FP64 inputs use FP64.
+struct FF {
+  float hi, lo;
+};
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bv = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bv)), __fsub_rn(b, bv));
+}
+
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+  p = __fmul_rn(a, b);
+  e = __fmaf_rn(a, b, -p);
+}
+
+// r[0] x + r[1] y + r[2] z as hi + lo (hi = the sum rounded once).
+__device__ __forceinline__ FF dot3(const float* r, float x, float y, float z) {
+  float p, s, h, e, q;
+  two_prod(r[0], x, p, s);
+  two_prod(r[1], y, h, e);
+  two_sum(p, h, p, q);
+  s = __fadd_rn(s, __fadd_rn(q, e));
+  two_prod(r[2], z, h, e);
+  two_sum(p, h, p, q);
+  s = __fadd_rn(s, __fadd_rn(q, e));
+  FF out;
+  two_sum(p, s, out.hi, out.lo);
+  return out;
+}
+
+// Above the horizon: topocentric z > 0 (hi has the sign of hi + lo).
+__device__ __forceinline__ bool above_horizon(const float* rot, float x, float y, float z) {
+  return dot3(rot + 6, x, y, z).hi > 0.f;
+}
+__device__ __forceinline__ bool above_horizon(const double* rot, double x, double y, double z) {
+  return fma(rot[6], x, fma(rot[7], y, rot[8] * z)) > 0.0;
 }
 
 // Source block bx of time tt: sources above the horizon, into
@@ -170,13 +215,13 @@ template <typename R>
 __device__ __forceinline__ void prep_count_block(const R* __restrict__ crd_eq, int nsrc,
                                                  const R* __restrict__ eq2tops, int t0, int nblk,
                                                  int* __restrict__ block_counts, int bx, int tt,
-                                                 double* rot, int* warp_cnt) {
+                                                 R* rot, int* warp_cnt) {
   load_rot(eq2tops, t0 + tt, rot);
   __syncthreads();
   const int s = bx * kPrepBlock + threadIdx.x;
   bool up = false;
   if (s < nsrc)
-    up = top_z(rot, crd_eq[s], crd_eq[(size_t)nsrc + s], crd_eq[2 * (size_t)nsrc + s]) > 0.0;
+    up = above_horizon(rot, crd_eq[s], crd_eq[(size_t)nsrc + s], crd_eq[2 * (size_t)nsrc + s]);
   const unsigned m = __ballot_sync(0xffffffffu, up);
   if ((threadIdx.x & 31) == 0) warp_cnt[threadIdx.x >> 5] = __popc(m);
   __syncthreads();
@@ -191,27 +236,17 @@ template <typename R>
 __global__ void __launch_bounds__(kPrepBlock)
 prep_count_kernel(const R* __restrict__ crd_eq, int nsrc, const R* __restrict__ eq2tops,
                   int t0, int nblk, int* __restrict__ block_counts) {
-  __shared__ double rot[9];
+  __shared__ R rot[9];
   __shared__ int warp_cnt[kPrepBlock / 32];
   prep_count_block<R>(crd_eq, nsrc, eq2tops, t0, nblk, block_counts, blockIdx.x, blockIdx.y, rot,
                       warp_cnt);
 }
 
-__device__ __forceinline__ void fill_rec(SrcRec32& r, double x, double y, double z,
-                                         double amp, int pix, double fx, double fy) {
-  r.sx = (float)x; r.sy = (float)y; r.sz = (float)z; r.amp = (float)amp;
-  r.pix = pix; r.fx = (float)fx; r.fy = (float)fy; r.pad = 0;
-}
-__device__ __forceinline__ void fill_rec(SrcRec64& r, double x, double y, double z,
-                                         double amp, int pix, double fx, double fy) {
-  r.sx = x; r.sy = y; r.sz = z; r.amp = amp; r.fx = fx; r.fy = fy; r.pix = pix;
-  r.pad[0] = r.pad[1] = r.pad[2] = 0;
-}
-
 // Lower corner and weight along one beam axis, clamped so that the four
 // gathered texels always lie inside the P x P grid.  Outside the grid the
 // value is the edge texel's, as with the reference's clamped texture
-// (vis.py:39) and RectBivariateSpline (test_vis_gpu.py:334).
+// (vis.py:39) and RectBivariateSpline (test_vis_gpu.py:334).  The texel
+// coordinate is b = (P - 1)(c / 2 + 1 / 2) (vis.py:63-73).
 __device__ __forceinline__ int beam_axis(double c, int P, double& w) {
   const double b = (P - 1) * fma(0.5, c, 0.5);
   const double fb = floor(b);
@@ -222,10 +257,56 @@ __device__ __forceinline__ int beam_axis(double c, int P, double& w) {
   return (int)fmin(fmax(fb, 0.0), (double)(P - 2));
 }
 
+// The same from c = hi + lo in FP32: b = h (c + 1), h = (P - 1) / 2 (exact),
+// carried as b + be; b - floor(b) is exact, and the weight is rounded once.
+__device__ __forceinline__ int beam_axis(FF c, int P, float& w) {
+  const float h = 0.5f * (float)(P - 1);
+  float u, ue, b, be;
+  two_sum(c.hi, 1.f, u, ue);
+  ue = __fadd_rn(ue, c.lo);
+  two_prod(h, u, b, be);
+  be = __fmaf_rn(h, ue, be);
+  float fb = floorf(b);
+  float f = __fadd_rn(__fsub_rn(b, fb), be);
+  if (f < 0.f) {  // b + be lies just below the integer b
+    fb -= 1.f;
+    f = __fadd_rn(f, 1.f);
+  } else if (f >= 1.f) {
+    fb += 1.f;
+    f = __fsub_rn(f, 1.f);
+  }
+  w = f;
+  if (P < 2) { w = 0.f; return 0; }
+  if (fb < 0.f) w = 0.f;
+  if (fb >= (float)(P - 1)) w = 1.f;
+  return (int)fminf(fmaxf(fb, 0.f), (float)(P - 2));
+}
+
+// The record of a source above the horizon: its direction, sqrt(I) (sqrtf
+// is correctly rounded, as is the FP64 square root rounded to FP32), and
+// its beam corner and weights.
+__device__ __forceinline__ void fill_rec(SrcRec32& r, const float* rot, float x, float y,
+                                         float z, float I, int P) {
+  float fx, fy;
+  const int px = beam_axis(dot3(rot, x, y, z), P, fx);
+  const int py = beam_axis(dot3(rot + 3, x, y, z), P, fy);
+  r.sx = x; r.sy = y; r.sz = z; r.amp = sqrtf(I);
+  r.pix = py * P + px; r.fx = fx; r.fy = fy; r.pad = 0;
+}
+__device__ __forceinline__ void fill_rec(SrcRec64& r, const double* rot, double x, double y,
+                                         double z, double I, int P) {
+  double fx, fy;
+  const int px = beam_axis(fma(rot[0], x, fma(rot[1], y, rot[2] * z)), P, fx);
+  const int py = beam_axis(fma(rot[3], x, fma(rot[4], y, rot[5] * z)), P, fy);
+  r.sx = x; r.sy = y; r.sz = z; r.amp = sqrt(I); r.fx = fx; r.fy = fy; r.pix = py * P + px;
+  r.pad[0] = r.pad[1] = r.pad[2] = 0;
+}
+
 // Source block bx of time tt: records of its sources above the horizon at
 // their place in catalogue order (after the blocks before it).
+template <typename R>
 struct PrepWriteSmem {
-  double rot[9];
+  R rot[9];
   int warp_cnt[kPrepBlock / 32];
   int red[kPrepBlock / 32];
   int base;
@@ -238,8 +319,8 @@ __device__ __forceinline__ void prep_write_block(const R* __restrict__ crd_eq,
                                                  const int* __restrict__ block_counts,
                                                  typename Traits<R>::Rec* __restrict__ rec,
                                                  int* __restrict__ count, int bx, int tt,
-                                                 PrepWriteSmem& sm) {
-  double* rot = sm.rot;
+                                                 PrepWriteSmem<R>& sm) {
+  R* rot = sm.rot;
   int* warp_cnt = sm.warp_cnt;
   int* red = sm.red;
   int& base = sm.base;
@@ -257,15 +338,12 @@ __device__ __forceinline__ void prep_write_block(const R* __restrict__ crd_eq,
     if (threadIdx.x == 0) base = c;
   }
   const int s = bx * kPrepBlock + threadIdx.x;
-  double x = 0, y = 0, z = 0, tx = 0, ty = 0, tz = 0;
+  R x = 0, y = 0, z = 0;
   bool up = false;
   __syncthreads();
   if (s < nsrc) {
     x = crd_eq[s]; y = crd_eq[(size_t)nsrc + s]; z = crd_eq[2 * (size_t)nsrc + s];
-    tx = fma(rot[0], x, fma(rot[1], y, rot[2] * z));
-    ty = fma(rot[3], x, fma(rot[4], y, rot[5] * z));
-    tz = top_z(rot, x, y, z);
-    up = tz > 0.0;
+    up = above_horizon(rot, x, y, z);
   }
   const unsigned m = __ballot_sync(0xffffffffu, up);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -284,11 +362,8 @@ __device__ __forceinline__ void prep_write_block(const R* __restrict__ crd_eq,
   __syncthreads();
   if (up) {
     const int idx = base + red[warp] + __popc(m & ((1u << lane) - 1u));
-    double fx, fy;
-    const int px = beam_axis(tx, P, fx);
-    const int py = beam_axis(ty, P, fy);
     typename Traits<R>::Rec r;
-    fill_rec(r, x, y, z, sqrt((double)I_sky[s]), py * P + px, fx, fy);
+    fill_rec(r, rot, x, y, z, I_sky[s], P);
     rec[(size_t)tt * rec_stride + idx] = r;
   }
 }
@@ -299,7 +374,7 @@ prep_write_kernel(const R* __restrict__ crd_eq, const R* __restrict__ I_sky, int
                   size_t rec_stride, const R* __restrict__ eq2tops, int t0, int nblk, int P,
                   const int* __restrict__ block_counts,
                   typename Traits<R>::Rec* __restrict__ rec, int* __restrict__ count) {
-  __shared__ PrepWriteSmem sm;
+  __shared__ PrepWriteSmem<R> sm;
   prep_write_block<R>(crd_eq, I_sky, nsrc, rec_stride, eq2tops, t0, nblk, P, block_counts, rec,
                       count, blockIdx.x, blockIdx.y, sm);
 }
@@ -527,7 +602,7 @@ __device__ __forceinline__ void batch_catalogue(const PrepSim& sm, const float*&
 __global__ void __launch_bounds__(kPrepBlock)
 prep_count_batch_kernel(const PrepSim* __restrict__ sims, int nsims,
                         const long long* __restrict__ pre) {
-  __shared__ double rot[9];
+  __shared__ float rot[9];
   __shared__ int warp_cnt[kPrepBlock / 32];
   const int si = find_segment(pre, nsims, blockIdx.x);
   const PrepSim& sm = sims[si];
@@ -542,7 +617,7 @@ prep_count_batch_kernel(const PrepSim* __restrict__ sims, int nsims,
 __global__ void __launch_bounds__(kPrepBlock)
 prep_write_batch_kernel(const PrepSim* __restrict__ sims, int nsims,
                         const long long* __restrict__ pre) {
-  __shared__ PrepWriteSmem smw;
+  __shared__ PrepWriteSmem<float> smw;
   const int si = find_segment(pre, nsims, blockIdx.x);
   const PrepSim& sm = sims[si];
   const int nblk = prep_blocks_of(sm.S);
