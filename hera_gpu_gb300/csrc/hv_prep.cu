@@ -15,6 +15,7 @@
 //    (the reference computes them and multiplies by A = 0); the survivors keep
 //    their input order, so the split-K order is deterministic.
 #include <algorithm>
+#include <type_traits>
 
 #include "hv_internal.cuh"
 #include "hv_kernels.h"
@@ -302,14 +303,65 @@ __device__ __forceinline__ void fill_rec(SrcRec64& r, const double* rot, double 
   r.pad[0] = r.pad[1] = r.pad[2] = 0;
 }
 
-// Source block bx of time tt: records of its sources above the horizon at
-// their place in catalogue order (after the blocks before it).
+// Ascending bitonic sort of the first n keys of a block (n a power of two,
+// 32 <= n <= blockDim.x, the same in every thread): thread i < n returns the
+// i-th smallest; the others return their v.  Exchanges at distance >= 32 go
+// through sk, shorter ones through warp shuffles.
+__device__ __forceinline__ uint32_t block_sort(uint32_t v, uint32_t* sk, int n) {
+  const int i = threadIdx.x;
+  const bool act = i < n;
+#pragma unroll 1
+  for (int k = 2; k <= n; k <<= 1) {
+#pragma unroll 1
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      uint32_t o;
+      if (j >= 32) {
+        if (act) sk[i] = v;
+        __syncthreads();
+        o = act ? sk[i ^ j] : v;
+        __syncthreads();
+      } else {
+        o = __shfl_xor_sync(0xffffffffu, v, j);
+      }
+      // the lower index of a pair keeps the minimum when the pair sorts
+      // ascending ((i & k) == 0), the maximum otherwise
+      const bool keep_min = ((i & j) == 0) == ((i & k) == 0);
+      if (act) v = keep_min ? min(v, o) : max(v, o);
+    }
+  }
+  return v;
+}
+
+static_assert(kPrepBlock <= 1024, "a key holds 10 bits of index within the block");
+// Beams up to this size are written in pixel order (a key holds the pixel in
+// its upper 22 bits).
+constexpr int kPixelOrderMaxP = 2048;
+
+// FP32 records pass through shared memory so that a block writes them in
+// beam-pixel order (sources of one pixel in catalogue order).
+template <typename R>
+struct PrepOrder {};
+template <>
+struct PrepOrder<float> {
+  uint32_t key[kPrepBlock];
+  SrcRec32 rec[kPrepBlock];
+};
+
+// Source block bx of time tt: records of its sources above the horizon, at
+// the block's place in the time's list (after the blocks before it).  FP32
+// records of beams up to kPixelOrderMaxP pixels a side are written in
+// beam-pixel order within the block (ties in catalogue order): the
+// catalogue is in spatial order, so a block covers a few neighbouring beam
+// pixels, and in pixel order most units of 8 consecutive records share one
+// pixel (the fused kernel then loads that pixel's four corners once per
+// unit).  Other records keep catalogue order.
 template <typename R>
 struct PrepWriteSmem {
   R rot[9];
   int warp_cnt[kPrepBlock / 32];
   int red[kPrepBlock / 32];
-  int base;
+  int base, total;
+  PrepOrder<R> ord;
 };
 template <typename R>
 __device__ __forceinline__ void prep_write_block(const R* __restrict__ crd_eq,
@@ -357,9 +409,31 @@ __device__ __forceinline__ void prep_write_block(const R* __restrict__ crd_eq,
       if (lane >= o) incl += n;
     }
     red[lane] = incl - c;
+    if (lane == 31) sm.total = incl;
     if (bx == nblk - 1 && lane == 31) count[tt] = base + incl;
   }
   __syncthreads();
+  if constexpr (std::is_same<R, float>::value) {
+    if (P <= kPixelOrderMaxP) {
+      // the block's records and keys (pixel, catalogue rank), compacted
+      const int total = sm.total;
+      if (up) {
+        const int c = red[warp] + __popc(m & ((1u << lane) - 1u));
+        SrcRec32 r;
+        fill_rec(r, rot, x, y, z, I_sky[s], P);
+        sm.ord.rec[c] = r;
+        sm.ord.key[c] = ((uint32_t)r.pix << 10) | (uint32_t)c;
+      }
+      __syncthreads();
+      int n = 32;
+      while (n < total) n <<= 1;
+      uint32_t key = (int)threadIdx.x < total ? sm.ord.key[threadIdx.x] : 0xffffffffu;
+      key = block_sort(key, sm.ord.key, n);
+      if ((int)threadIdx.x < total)
+        rec[(size_t)tt * rec_stride + base + threadIdx.x] = sm.ord.rec[key & (kPrepBlock - 1)];
+      return;
+    }
+  }
   if (up) {
     const int idx = base + red[warp] + __popc(m & ((1u << lane) - 1u));
     typename Traits<R>::Rec r;

@@ -17,24 +17,32 @@
 //   K-step: the column blocks sit side by side in shared memory, so the row
 //   block's operand is read once for both pairs.  Its accumulators -- Re V
 //   in TMEM columns [0, 256), Im V in [256, 512) -- fill the 512 columns.
-//   A work item is (time, frequency, source chunk, group).  Items are taken
-//   round-robin by a grid of one CTA per SM; each item's partial sum over its
-//   source chunk goes to HBM and a separate kernel reduces the chunks in a
-//   fixed order (deterministic split-K over sources).
+//   A work item is (time, frequency, source chunk, group); in cluster mode
+//   (2-8 groups: 129-640 antennas) an item is (time, frequency, chunk) for a
+//   thread-block cluster of one CTA per group, and each antenna block is
+//   generated once per cluster, by the CTA that owns it, and pushed to the
+//   peers that also use it.  A persistent grid of one CTA (or cluster) per
+//   SM claims items at run time from a device counter.  Each item's partial
+//   sum over its source chunk goes to HBM and a separate kernel reduces the
+//   chunks in a fixed order (deterministic split-K over sources).
 //
-// Pipeline inside a CTA (608 threads)
-//   warp 16       TMA producer: 16 source records per stage, one 2-D
-//                 cp.async.bulk.tensor into shared memory.
-//   warps 0-15    phasor generators, in two teams of 8 warps that take
-//                 alternate stages: for each (slot, antenna row, 8 sources)
-//                 the bilinear beam (4 coalesced gathers: lanes are
-//                 antennas), the phase in cycles reduced exactly in FP32
+// Pipeline inside a CTA (split BF16: 12 + 3 warps; FP16 + FP8: 16 + 3)
+//   generator warps  phasor generators, in teams that take stages in turn:
+//                 for each (slot, antenna row, unit of 8 sources) the
+//                 bilinear beam (4 coalesced gathers: lanes are antennas),
+//                 the phase in cycles reduced exactly in FP32
 //                 (phase_cycles32), sincos, v = A sqrt(I) e^{2 pi i phi},
-//                 split v = hi + lo in BF16, stored to the canonical K-major
-//                 128-byte-swizzled UMMA layout.  After the last stage of an
-//                 item they drain TMEM to the partial buffer (epilogue).
-//   warp 17       MMA issuer (one thread) and TMEM owner.
-//   warp 18       cluster mode: pushes this CTA's tiles to peer CTAs.
+//                 the split of v, stored to the canonical K-major
+//                 128-byte-swizzled UMMA layout.  Every TC_FLUSH_SOURCES
+//                 sources of an item, and after its last stage, they drain
+//                 TMEM into the item's partial buffer (epilogue).
+//   next warp     TMA producer: each stage's source records, one 2-D
+//                 cp.async.bulk.tensor into shared memory.  Its first thread
+//                 (in cluster mode, rank 0's) claims the items into a ring
+//                 of item indices in shared memory that every role of every
+//                 CTA of the cluster reads.
+//   next warp     MMA issuer (one thread) and TMEM owner.
+//   last warp     cluster mode: pushes this CTA's tiles to peer CTAs.
 //
 // Operand layout of one stage (16 sources): one tile per slot, the slots'
 // tiles side by side (16 KB each: 128 rows x 128 bytes, K = 64 BF16 per
@@ -98,7 +106,6 @@ template <> struct TcForm<1> {
   static constexpr int KS = 32, TILES = 2, NREC = TC_NREC_ALL;
 };
 constexpr int TC_KS_MAX = 32;
-constexpr int TC_REC_MAX = TC_KS_MAX * 32;  // bytes of source records per stage (largest form)
 // Record stages: more than operand stages (they are small), so the TMA
 // producer runs further ahead and a generator warp finds its next records
 // loaded even while slower warps still hold earlier stages.
