@@ -646,27 +646,34 @@ __device__ __forceinline__ void gen_unit_path(const SrcRec32* rec, const Ucoef32
                                               const float* beam_a, int Np, int dx, int dy,
                                               float4 ref, float ph_ref, float csc, float* rv,
                                               float* iv) {
-  float c00 = 0.f, c01 = 0.f, c10 = 0.f, c11 = 0.f;
+  // one pixel for the unit: its corners as c00 + fx d1 + fy (d2 + fx d3),
+  // the bilinear interpolant with the differences formed once per unit
+  float c00 = 0.f, d1 = 0.f, d2 = 0.f, d3 = 0.f;
   if (kOnePixel) {
     const float* bp = beam_a + (size_t)__float_as_int(reinterpret_cast<const float4*>(rec)[1].x) * Np;
     c00 = __ldg(bp);
-    c01 = __ldg(bp + (size_t)dx * Np);
-    c10 = __ldg(bp + (size_t)dy * Np);
-    c11 = __ldg(bp + (size_t)(dx + dy) * Np);
+    const float c01 = __ldg(bp + (size_t)dx * Np);
+    const float c10 = __ldg(bp + (size_t)dy * Np);
+    const float c11 = __ldg(bp + (size_t)(dx + dy) * Np);
+    d1 = c01 - c00;
+    d2 = c10 - c00;
+    d3 = (c11 - c10) - d1;
   }
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
     const float4* rp = reinterpret_cast<const float4*>(rec + q);
     const float4 ra = rp[0], rb = rp[1];  // sx sy sz amp | pix fx fy -
-    float b00 = c00, b01 = c01, b10 = c10, b11 = c11;
-    if (!kOnePixel) {
+    float A;
+    if (kOnePixel) {
+      A = fmaf(rb.z, fmaf(rb.y, d3, d2), fmaf(rb.y, d1, c00));
+    } else {
       const float* bp = beam_a + (size_t)__float_as_int(rb.x) * Np;
-      b00 = __ldg(bp);
-      b01 = __ldg(bp + (size_t)dx * Np);
-      b10 = __ldg(bp + (size_t)dy * Np);
-      b11 = __ldg(bp + (size_t)(dx + dy) * Np);
+      const float b00 = __ldg(bp);
+      const float b01 = __ldg(bp + (size_t)dx * Np);
+      const float b10 = __ldg(bp + (size_t)dy * Np);
+      const float b11 = __ldg(bp + (size_t)(dx + dy) * Np);
+      A = lerp(lerp(b00, b01, rb.y), lerp(b10, b11, rb.y), rb.z);
     }
-    const float A = lerp(lerp(b00, b01, rb.y), lerp(b10, b11, rb.y), rb.z);
     float ph;
     if (!kNear) {
       ph = phase_exact(uc, ra.x, ra.y, ra.z);
