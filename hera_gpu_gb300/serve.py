@@ -333,11 +333,21 @@ def summarize(requests, wall_s):
     done = [r for r in requests if r.ok]
     lat = np.array([r.latency for r in done]) if done else np.zeros(1)
     vis = sum(r.visibilities for r in done)
+    # steady state: the p99 of the requests that arrived in the first and in
+    # the second half of the run (a loop that keeps up shows no growth)
+    by_arrival = sorted(done, key=lambda r: r.arrival)
+    half = len(by_arrival) // 2
+
+    def p99(rs):
+        return float(np.percentile([r.latency for r in rs], 99) * 1e3) if rs else 0.0
+
     return {"requests": len(requests), "served": len(done),
             "failed": sum(1 for r in requests if r.error and not r.cancelled),
             "cancelled": sum(1 for r in requests if r.cancelled),
             "p50_ms": float(np.percentile(lat, 50) * 1e3),
             "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "p99_first_half_ms": p99(by_arrival[:half]),
+            "p99_second_half_ms": p99(by_arrival[half:]),
             "mean_ms": float(lat.mean() * 1e3), "vis_per_s": vis / wall_s, "wall_s": wall_s}
 
 

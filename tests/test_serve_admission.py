@@ -179,3 +179,17 @@ def test_batch_chunk_matches_the_library():
     # admission counts split-K partials with the library's chunk size
     src = open(os.path.join(os.path.dirname(serve.__file__), "csrc", "hv_batch.cu")).read()
     assert int(re.search(r"constexpr int kBatchChunk = (\d+);", src).group(1)) == serve.BATCH_CHUNK
+
+
+def test_summary_splits_p99_by_arrival_half():
+    # a queue that grows: the later arrivals wait longer
+    reqs = []
+    for i in range(100):
+        r = request(i, 1000, arrival=0.01 * i)
+        r.t_done = r.arrival + (0.01 if i < 50 else 0.5 + 0.01 * i)
+        r.result = np.zeros(1)
+        reqs.append(r)
+    stats = serve.summarize(reqs, 2.0)
+    assert stats["served"] == 100
+    assert abs(stats["p99_first_half_ms"] - 10.0) < 1e-6
+    assert stats["p99_second_half_ms"] > 1000.0
