@@ -384,10 +384,10 @@ def load_peaks():
 # fused-kernel launch, measured once with ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum of the launch on 350 antennas x 1,048,576 sources x
 # 16 channels x 4 LSTs, which under ncu computes all 33,517,808 units:
-# split BF16 2.358 GB, FP16 + FP8 2.564 GB): the bench cannot read DRAM
+# split BF16 2.367 GB, FP16 + FP8 2.615 GB): the bench cannot read DRAM
 # counters itself, so the figure is carried here and scaled by the units
 # each timed launch processed.
-TC_DRAM_BYTES_PER_UNIT = {"tc": 70.355, "tc_fp16": 76.489}
+TC_DRAM_BYTES_PER_UNIT = {"tc": 70.619, "tc_fp16": 78.013}
 
 
 def run_ours(args):
