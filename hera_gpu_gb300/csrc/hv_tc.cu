@@ -812,8 +812,8 @@ __device__ __forceinline__ bool decode_item(const TcParams& p, long long it, int
   return true;
 }
 
-// 19 warps on 4 schedulers: the busiest scheduler holds 5 warps, and its
-// 16K-register file caps a thread at 96 registers (launch bounds give that).
+// One CTA per SM; the launch bounds give each form's register budget (split
+// BF16: 15 warps, 128 registers a thread; FP16 + FP8: 19 warps, 96).
 template <bool kCluster, bool kTable, int kForm>
 __global__ void __launch_bounds__(tc_threads<kForm>(), 1)
 tc_vis_kernel(const __grid_constant__ CUtensorMap rec_map, const __grid_constant__ TcParams p) {
@@ -1485,7 +1485,7 @@ int tc_fill_group_table(int nant, void* host_buf) {
 
 int tc_chunk_sources(int nsrc, int nslices, int ngroups, int num_sms) {
   // about 40 items per cluster (or per CTA without clusters), so that the
-  // round-robin hand-out leaves a short tail, in chunks of 1k-16k sources
+  // run-time claiming leaves a short tail, in chunks of 1k-16k sources
   // (about half the catalogue is above the horizon)
   const long long nchunk =
       std::max<long long>(1, (40LL * num_sms + (long long)nslices * ngroups - 1) /
