@@ -616,25 +616,36 @@ def run_ours(args):
                       f"linearly to {S}; value_fp64: the float64 oracle of one whole slice "
                       f"({S} sources) on {cores} processes"}
 
+    # The legs after the headline each report their own failure (a library
+    # error, a device-side wait that gave up) in their object instead of
+    # taking the line down with them.
+    def leg(fn, *a):
+        try:
+            return fn(*a)
+        except Exception as e:  # noqa: BLE001 -- reported in the JSON line
+            import traceback
+            traceback.print_exc()
+            return {"error": f"{type(e).__name__}: {e}"}
+
     # ---- the small and array-scale configurations ---------------------------
     if rank == 0 and not args.no_configs:
-        line["configs"] = run_configs(args, local, pool, cores)
+        line["configs"] = leg(run_configs, args, local, pool, cores)
 
     # ---- batched form: many uneven simulations in one plan ----------------
     if rank == 0 and args.batch_sims > 0:
-        line["batch"] = run_batch(args, local)
+        line["batch"] = leg(run_batch, args, local)
 
     # ---- the 2-D median filter (hera_gpu.MedianFilter) ---------------------
     if rank == 0 and not args.no_median:
-        line["median"] = run_median(args, local)
+        line["median"] = leg(run_median, args, local)
 
     # ---- Omnical redundant calibration (hera_gpu.redcal.omnical) -----------
     if rank == 0 and not args.no_omnical:
-        line["omnical"] = run_omnical(args, local)
+        line["omnical"] = leg(run_omnical, args, local)
 
     # ---- serving: Poisson request stream, continuous batching --------------
     if rank == 0 and args.serve_requests > 0:
-        line["serve"] = run_serve(args, local, pool)
+        line["serve"] = leg(run_serve, args, local, pool)
 
     if pool is not None:
         pool.close()

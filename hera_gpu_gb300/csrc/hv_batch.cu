@@ -463,6 +463,18 @@ int hv_batch_create(hv_context* ctx, const hv_sim* sims, int nsims, unsigned fla
               cudaEventSynchronize(e1);
               cudaEventElapsedTime(&ms, e0, e1);
             }
+            // a candidate whose device-side waits gave up is never chosen,
+            // and its flag does not carry over to the batch's own runs
+            int flag = 0;
+            if (r == HV_OK &&
+                (cudaMemcpyAsync(&flag, b->d_err, sizeof(int), cudaMemcpyDeviceToHost, st) !=
+                     cudaSuccess ||
+                 cudaStreamSynchronize(st) != cudaSuccess))
+              r = HV_ERR_CUDA;
+            if (flag) {
+              cudaMemsetAsync(b->d_err, 0, sizeof(int), st);
+              ms = 1e30f;
+            }
             if (r == HV_OK && ms < best_ms[c]) {
               best_ms[c] = ms;
               best_div[c] = div;
@@ -536,7 +548,10 @@ int hv_batch_sync(hv_batch* b) {
     return HV_ERR_CUDA;
   if (flag) {
     cudaMemsetAsync(b->d_err, 0, sizeof(int), st);
-    return flag == 2 ? HV_ERR_ARG : flag == 3 ? HV_ERR_UNSUPPORTED : HV_ERR_TIMEOUT;
+    if (flag == 2 || flag == 3) return flag == 2 ? HV_ERR_ARG : HV_ERR_UNSUPPORTED;
+    hv_context_set_error(b->ctx, "a device-side wait of the batch gave up; results of the "
+                                 "last launch are invalid");
+    return HV_ERR_TIMEOUT;
   }
   return HV_OK;
 }
