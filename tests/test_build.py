@@ -8,7 +8,7 @@ flags (``nvcc -Xptxas -v``; it cross-compiles for sm_103a, no GPU is used).
   runs 15 warps, at most 4 on each of the SM's 4 schedulers, so a thread may
   hold 128 registers, and spills at most 64 bytes; the FP16 + FP8 form runs
   19 warps, so the busiest scheduler holds 5 and a thread 96 registers, and
-  spills 96-150 bytes.  A change that spills more would slow the
+  spills at most 152 bytes.  A change that spills more would slow the
   latency-bound phasor generators.
 """
 import concurrent.futures as cf
