@@ -221,7 +221,7 @@ class Context:
         self.check(self.lib.hv_set_profiling(self.h, 1 if enable else 0))
 
     def set_wait_limit(self, wait_s: float = 0.0, stall: bool = False):
-        """Limit of each device-side wait of the fused kernel (0: 2 s); with
+        """Limit of each device-side wait of the fused kernel (0: 10 s); with
         ``stall`` the next fused launches are made to time out (fault
         injection for tests of failure detection)."""
         self.check(self.lib.hv_set_wait_limit(self.h, int(wait_s * 1e9), 1 if stall else 0))

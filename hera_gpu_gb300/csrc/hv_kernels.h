@@ -188,7 +188,7 @@ cudaError_t tc_configure();
 // all.  d_table / h_table: device and host (kept alive until the copy ran)
 // buffers of tc_sim_table_bytes(nsims).  Cluster mode is used when every
 // simulation has the same clusterable group layout.  wait_ns: limit of
-// each device-side wait (0: 2 s); stall: fault injection (the first record
+// each device-side wait (0: 10 s); stall: fault injection (the first record
 // copy is never issued, so the launch ends with a timeout status).
 // share (one simulation in cluster mode): the SMs no cluster fits on run a
 // share of the items in a second, concurrent launch (forked from st onto

@@ -152,7 +152,10 @@ static_assert(TC_MAX_STAGES <= TC_NREC_ALL, "record stages >= operand stages");
 static_assert(TC_FLUSH_SOURCES % TC_KS_MAX == 0, "flush interval: whole stages of every form");
 constexpr int TC_TMEM_COLS = 512;
 constexpr int TC_SMEM_LIMIT = 227 * 1024;
-constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // default limit of one wait: 2 s
+// default limit of one wait: 10 s, far above any wait of a working launch
+// (an item lasts milliseconds), so that a disturbance of the timer the
+// waits read cannot end a healthy wait
+constexpr unsigned long long TC_WAIT_NS = 10000000000ull;
 
 constexpr int kErrTimeout = 1;
 constexpr int kErrRange = 2;    // |U| beyond the exact range of rint_magic

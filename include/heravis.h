@@ -127,7 +127,7 @@ int hv_set_profiling(hv_context* ctx, int enable);
 int hv_profile_read(hv_context* ctx, double* ms, uint64_t* launches);
 
 /* Limit of each device-side wait of the fused kernel in this context
- * (wait_ns = 0: 2 s), and fault injection for tests of failure detection:
+ * (wait_ns = 0: 10 s), and fault injection for tests of failure detection:
  * with stall set, the next fused launches never issue their first source
  * copy, so their consumers' bounded waits run out and the call returns
  * HV_ERR_TIMEOUT with the context still usable.  No counterpart in the
