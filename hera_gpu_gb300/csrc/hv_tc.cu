@@ -1488,14 +1488,14 @@ int tc_fill_group_table(int nant, void* host_buf) {
 
 int tc_chunk_sources(int nsrc, int nslices, int ngroups, int num_sms) {
   // about 40 items per cluster (or per CTA without clusters), so that the
-  // run-time claiming leaves a short tail, in chunks of 1k-16k sources
+  // run-time claiming leaves a short tail, in chunks of 1k-32k sources
   // (about half the catalogue is above the horizon)
   const long long nchunk =
       std::max<long long>(1, (40LL * num_sms + (long long)nslices * ngroups - 1) /
                                  ((long long)nslices * ngroups));
   const long long up = std::max(nsrc / 2, 1);
   long long c = (up + nchunk - 1) / nchunk;
-  c = std::min<long long>(16384, std::max<long long>(1024, c));
+  c = std::min<long long>(32768, std::max<long long>(1024, c));
   c = (c + 31) / 32 * 32;
   return (int)c;
 }
