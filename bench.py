@@ -386,7 +386,11 @@ def load_peaks():
 # 16 channels x 4 LSTs, which under ncu computes all 33,517,808 units:
 # split BF16 2.367 GB, FP16 + FP8 2.615 GB): the bench cannot read DRAM
 # counters itself, so the figure is carried here and scaled by the units
-# each timed launch processed.
+# each timed launch processed.  That launch uses split-K chunks of 16384
+# sources; the 64-channel benchmark call uses chunks of 32768, with half
+# as many partial sums to write, so for it the figure is an upper bound
+# (a full-size capture of these counters takes several ncu passes, more
+# than a capture of that size may).
 TC_DRAM_BYTES_PER_UNIT = {"tc": 70.619, "tc_fp16": 78.013}
 
 
