@@ -394,6 +394,19 @@ def load_peaks():
 TC_DRAM_BYTES_PER_UNIT = {"tc": 70.619, "tc_fp16": 78.013}
 
 
+def run_leg(fn, *a):
+    """One leg of the line after the headline: its result, or its failure (a
+    library error, a device-side wait that gave up) reported in its own
+    object instead of taking the whole line down (the traceback goes to
+    stderr)."""
+    try:
+        return fn(*a)
+    except Exception as e:  # noqa: BLE001 -- reported in the JSON line
+        import traceback
+        traceback.print_exc()
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
 def run_ours(args):
     import numpy as np
     world, rank, local = dist_setup()
@@ -620,16 +633,7 @@ def run_ours(args):
                       f"linearly to {S}; value_fp64: the float64 oracle of one whole slice "
                       f"({S} sources) on {cores} processes"}
 
-    # The legs after the headline each report their own failure (a library
-    # error, a device-side wait that gave up) in their object instead of
-    # taking the line down with them.
-    def leg(fn, *a):
-        try:
-            return fn(*a)
-        except Exception as e:  # noqa: BLE001 -- reported in the JSON line
-            import traceback
-            traceback.print_exc()
-            return {"error": f"{type(e).__name__}: {e}"}
+    leg = run_leg
 
     # ---- the small and array-scale configurations ---------------------------
     if rank == 0 and not args.no_configs:
