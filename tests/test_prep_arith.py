@@ -102,3 +102,40 @@ def test_fp32_geometry_matches_fp64(P):
             inside = (np.floor(b) == i32) & (np.floor(b) >= 0) & (np.floor(b) <= P - 2)
             err = np.abs(w32[inside].astype(L) - (b - np.floor(b))[inside])
             assert float(err.max()) <= 2.0 ** -24 * 1.25
+
+
+def _block_sort(keys, n, threads=1024):
+    """hv_prep.cu:block_sort restated: thread i < n keeps the minimum of the
+    pair (i, i ^ j) when its lower index sorts ascending ((i & k) == 0)."""
+    w = np.full(threads, 0xffffffff, dtype=np.uint64)
+    w[:len(keys)] = keys
+    i = np.arange(threads)
+    act = i < n
+    k = 2
+    while k <= n:
+        j = k >> 1
+        while j > 0:
+            o = np.where(act, w[np.where(act, i ^ j, i)], w)
+            keep_min = ((i & j) == 0) == ((i & k) == 0)
+            w = np.where(act, np.where(keep_min, np.minimum(w, o), np.maximum(w, o)), w)
+            j >>= 1
+        k <<= 1
+    return w
+
+
+@pytest.mark.parametrize("total", [0, 1, 7, 31, 32, 33, 100, 511, 512, 700, 1024])
+def test_pixel_order_sort_of_a_block(total):
+    """The records of a preparation block in beam-pixel order, ties in
+    catalogue order: keys (pixel << 10 | rank), a network of the smallest
+    power of two >= max(total, 32) keys."""
+    rng = np.random.default_rng(total)
+    pix = rng.integers(0, 9, total).astype(np.uint64) + np.uint64(4000)
+    keys = (pix << np.uint64(10)) | np.arange(total, dtype=np.uint64)
+    n = 32
+    while n < total:
+        n <<= 1
+    out = _block_sort(keys, n)[:total]
+    np.testing.assert_array_equal(out, np.sort(keys))
+    order = (out & np.uint64(1023)).astype(int)
+    # stable: within a pixel, catalogue (rank) order
+    np.testing.assert_array_equal(order, np.lexsort((np.arange(total), pix)))
